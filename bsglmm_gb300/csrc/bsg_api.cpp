@@ -1,0 +1,924 @@
+// bsg_api.cpp -- host engine behind the C ABI of bsglmm_gb300.h: lattice
+// construction, uploads, chain state, the per-sweep launch plan, CUDA-graph
+// segments, status reporting and read-back.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/bsglmm_gb300.h"
+#include "bsg_internal.h"
+
+using namespace bsg;
+
+namespace {
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+struct Dataset {
+  int X = 0, Y = 0, Z = 0, PX = 0, PY = 0, nsize = 0;
+  int N = 0, P = 0, S = 0, V = 0, Vp = 0;
+  std::vector<int32_t> idx, idxsc, vox[2];
+  std::vector<uint8_t> nbrs[2];
+  std::vector<int32_t> pad_of_v;  // padded index of compact mask index v
+  DatasetDev dev{};               // device pointers
+};
+
+struct Chain {
+  int dataset = 0;
+  bsg_chain_desc desc{};
+  ChainDev dev{};
+};
+
+struct Group {
+  int P = 0;
+  std::vector<BlockMap> map[2];
+  BlockMap *d_map[2] = {nullptr, nullptr};
+};
+
+// Small per-chain counters kept together on the device.
+struct ChainCounters {
+  long long sweep;
+  long long nkept;
+  unsigned int done;
+  int status;
+};
+
+}  // namespace
+
+struct bsg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<cudaStream_t> side;
+  std::vector<cudaEvent_t> join;
+  cudaEvent_t fork = nullptr;
+  std::vector<Dataset> ds;
+  std::vector<Chain> ch;
+  std::vector<DevBuf> owned;
+  DatasetDev *d_ds = nullptr;
+  ChainDev *d_ch = nullptr;
+  size_t d_ds_cap = 0, d_ch_cap = 0;
+  bool plan_valid = false;
+  std::vector<Group> groups;
+  BlockMap *d_post_map = nullptr;
+  int post_blocks = 0;
+  int lpv = 1, threads = 128;
+  std::map<int64_t, cudaGraphExec_t> graphs;
+  std::string err;
+};
+
+namespace {
+
+bsg_status fail(bsg_ctx *c, bsg_status s, const std::string &m) {
+  if (c) c->err = m;
+  return s;
+}
+
+#define CK(call)                                                           \
+  do {                                                                     \
+    cudaError_t e_ = (call);                                               \
+    if (e_ != cudaSuccess)                                                 \
+      return fail(ctx, BSG_ERR_CUDA,                                       \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));     \
+  } while (0)
+
+void *dalloc(bsg_ctx *ctx, size_t bytes, cudaError_t *e) {
+  void *p = nullptr;
+  *e = cudaMalloc(&p, bytes ? bytes : 4);
+  if (*e != cudaSuccess) return nullptr;
+  ctx->owned.push_back({p, bytes});
+  return p;
+}
+
+void dfree(bsg_ctx *ctx, void *p) {
+  if (!p) return;
+  for (size_t i = 0; i < ctx->owned.size(); ++i)
+    if (ctx->owned[i].p == p) {
+      cudaFree(p);
+      ctx->owned.erase(ctx->owned.begin() + i);
+      return;
+    }
+}
+
+void clear_graphs(bsg_ctx *ctx) {
+  for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+  ctx->graphs.clear();
+}
+
+// Lattice of main.cu: padding by one voxel (main.cu:56), 6-neighbour
+// dilation (main.cu:189-205), compact maps in padded scan order
+// (main.cu:308-329), colour lists in interior scan order with colour 0 for
+// i+j+k odd in 1-based padded coordinates (main.cu:216-252,333-394) and
+// in-mask neighbour counts (cnt_nbrs, main.cu:471-502).
+void build_lattice(Dataset &d, const uint8_t *mask) {
+  const int X = d.X, Y = d.Y, Z = d.Z;
+  d.PX = X + 2;
+  d.PY = Y + 2;
+  const int PZ = Z + 2, sy = d.PX, sz = d.PX * d.PY;
+  d.nsize = d.PX * d.PY * PZ;
+  std::vector<uint8_t> msk(d.nsize, 0), mskp(d.nsize, 0);
+  size_t t = 0;
+  for (int k = 1; k <= Z; ++k)
+    for (int j = 1; j <= Y; ++j)
+      for (int i = 1; i <= X; ++i, ++t) msk[i + sy * j + sz * k] = mask[t] ? 1 : 0;
+  for (int k = 1; k <= Z; ++k)
+    for (int j = 1; j <= Y; ++j)
+      for (int i = 1; i <= X; ++i) {
+        const int p = i + sy * j + sz * k;
+        if (!msk[p]) continue;
+        mskp[p] = mskp[p - 1] = mskp[p + 1] = 1;
+        mskp[p - sy] = mskp[p + sy] = mskp[p - sz] = mskp[p + sz] = 1;
+      }
+  d.idx.assign(d.nsize, -1);
+  d.idxsc.assign(d.nsize, -1);
+  int cnt = 0, cntp = 0;
+  for (int p = 0; p < d.nsize; ++p) {
+    if (msk[p]) d.idx[p] = cnt++;
+    if (mskp[p]) d.idxsc[p] = cntp++;
+  }
+  d.V = cnt;
+  d.Vp = cntp;
+  d.pad_of_v.assign(d.V, 0);
+  for (int c = 0; c < 2; ++c) {
+    d.vox[c].clear();
+    d.nbrs[c].clear();
+  }
+  for (int k = 1; k <= Z; ++k)
+    for (int j = 1; j <= Y; ++j)
+      for (int i = 1; i <= X; ++i) {
+        const int p = i + sy * j + sz * k;
+        if (!msk[p]) continue;
+        d.pad_of_v[d.idx[p]] = p;
+        const int c = ((i + j + k) & 1) ? 0 : 1;
+        d.vox[c].push_back(p);
+        d.nbrs[c].push_back((uint8_t)(msk[p - 1] + msk[p + 1] + msk[p - sy] +
+                                      msk[p + sy] + msk[p - sz] + msk[p + sz]));
+      }
+}
+
+template <typename T>
+T *upload(bsg_ctx *ctx, const T *host, size_t n, cudaError_t *e) {
+  T *p = (T *)dalloc(ctx, sizeof(T) * n, e);
+  if (!p) return nullptr;
+  if (n) *e = cudaMemcpy(p, host, sizeof(T) * n, cudaMemcpyHostToDevice);
+  return *e == cudaSuccess ? p : nullptr;
+}
+
+bsg_status status_from_bits(int bits) {
+  if (!bits) return BSG_OK;
+  if (bits & kErrInput) return BSG_ERR_INVALID;
+  if (bits & kErrNaN) return BSG_ERR_NAN;
+  if (bits & (kErrChol | kErrWishart)) return BSG_ERR_NOT_SPD;
+  if (bits & (kErrTnCap | kErrGammaCap)) return BSG_ERR_SAMPLER_CAP;
+  return BSG_ERR_STATE;
+}
+
+std::string status_text(int bits) {
+  std::string s;
+  if (bits & kErrTnCap) s += " truncated-normal tail cap hit;";
+  if (bits & kErrGammaCap) s += " gamma cap hit;";
+  if (bits & kErrChol) s += " conditional precision of a voxel not SPD;";
+  if (bits & kErrWishart) s += " Wishart scale not SPD;";
+  if (bits & kErrNaN) s += " non-finite state;";
+  if (bits & kErrInput) s += " outcome values outside {0,1};";
+  return s;
+}
+
+// Rebuilds the device descriptor arrays and block maps.
+bsg_status build_plan(bsg_ctx *ctx) {
+  if (ctx->plan_valid) return BSG_OK;
+  if (ctx->ch.empty()) return fail(ctx, BSG_ERR_STATE, "no chain");
+  clear_graphs(ctx);
+  cudaError_t e;
+  if (ctx->d_ds_cap < ctx->ds.size()) {
+    dfree(ctx, ctx->d_ds);
+    ctx->d_ds_cap = ctx->ds.size() * 2;
+    ctx->d_ds = (DatasetDev *)dalloc(ctx, sizeof(DatasetDev) * ctx->d_ds_cap, &e);
+    CK(e);
+  }
+  if (ctx->d_ch_cap < ctx->ch.size()) {
+    dfree(ctx, ctx->d_ch);
+    ctx->d_ch_cap = ctx->ch.size() * 2;
+    ctx->d_ch = (ChainDev *)dalloc(ctx, sizeof(ChainDev) * ctx->d_ch_cap, &e);
+    CK(e);
+  }
+  std::vector<DatasetDev> hds;
+  for (auto &d : ctx->ds) hds.push_back(d.dev);
+  std::vector<ChainDev> hch;
+  for (auto &c : ctx->ch) hch.push_back(c.dev);
+  CK(cudaMemcpy(ctx->d_ds, hds.data(), sizeof(DatasetDev) * hds.size(),
+                cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_ch, hch.data(), sizeof(ChainDev) * hch.size(),
+                cudaMemcpyHostToDevice));
+  for (auto &g : ctx->groups)
+    for (int c = 0; c < 2; ++c) dfree(ctx, g.d_map[c]);
+  ctx->groups.clear();
+  const int vpb = ctx->threads / ctx->lpv;
+  for (size_t ci = 0; ci < ctx->ch.size(); ++ci) {
+    const Dataset &d = ctx->ds[ctx->ch[ci].dataset];
+    Group *g = nullptr;
+    for (auto &gg : ctx->groups)
+      if (gg.P == d.P) g = &gg;
+    if (!g) {
+      ctx->groups.push_back(Group());
+      g = &ctx->groups.back();
+      g->P = d.P;
+    }
+    for (int c = 0; c < 2; ++c)
+      for (int s = 0; s < (int)d.vox[c].size(); s += vpb)
+        g->map[c].push_back({(int32_t)ci, (int32_t)s});
+  }
+  for (auto &g : ctx->groups)
+    for (int c = 0; c < 2; ++c) {
+      g.d_map[c] = upload(ctx, g.map[c].data(), g.map[c].size(), &e);
+      CK(e);
+    }
+  std::vector<BlockMap> pm;
+  for (size_t ci = 0; ci < ctx->ch.size(); ++ci) {
+    const Dataset &d = ctx->ds[ctx->ch[ci].dataset];
+    const int ntot = d.V, per = kPostThreads * kPostPerThread;
+    for (int s = 0; s < ntot; s += per) pm.push_back({(int32_t)ci, (int32_t)s});
+  }
+  dfree(ctx, ctx->d_post_map);
+  ctx->d_post_map = upload(ctx, pm.data(), pm.size(), &e);
+  CK(e);
+  ctx->post_blocks = (int)pm.size();
+  while (ctx->side.size() < ctx->groups.size()) {
+    cudaStream_t s;
+    cudaEvent_t ev;
+    CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    ctx->side.push_back(s);
+    ctx->join.push_back(ev);
+  }
+  ctx->plan_valid = true;
+  return BSG_OK;
+}
+
+// Enqueues one sweep of every chain: per P group the two colour kernels
+// (groups on parallel branches when there are several), then the
+// post-sweep pass.
+cudaError_t enqueue_sweep(bsg_ctx *ctx, cudaStream_t st) {
+  const Supplied sup{};
+  cudaError_t e;
+  if (ctx->groups.size() == 1) {
+    const Group &g = ctx->groups[0];
+    for (int c = 0; c < 2; ++c) {
+      e = launch_fused(g.P, ctx->lpv, ctx->threads, false, ctx->d_ds,
+                       ctx->d_ch, g.d_map[c], (int)g.map[c].size(), c, sup, st);
+      if (e != cudaSuccess) return e;
+    }
+  } else {
+    if ((e = cudaEventRecord(ctx->fork, st)) != cudaSuccess) return e;
+    for (size_t gi = 0; gi < ctx->groups.size(); ++gi) {
+      const Group &g = ctx->groups[gi];
+      cudaStream_t s = ctx->side[gi];
+      if ((e = cudaStreamWaitEvent(s, ctx->fork, 0)) != cudaSuccess) return e;
+      for (int c = 0; c < 2; ++c) {
+        e = launch_fused(g.P, ctx->lpv, ctx->threads, false, ctx->d_ds,
+                         ctx->d_ch, g.d_map[c], (int)g.map[c].size(), c, sup, s);
+        if (e != cudaSuccess) return e;
+      }
+      if ((e = cudaEventRecord(ctx->join[gi], s)) != cudaSuccess) return e;
+      if ((e = cudaStreamWaitEvent(st, ctx->join[gi], 0)) != cudaSuccess) return e;
+    }
+  }
+  return launch_post(ctx->d_ds, ctx->d_ch, ctx->d_post_map, ctx->post_blocks,
+                     false, sup, st);
+}
+
+bsg_status get_graph(bsg_ctx *ctx, int64_t nsw, cudaGraphExec_t *out) {
+  auto it = ctx->graphs.find(nsw);
+  if (it != ctx->graphs.end()) {
+    *out = it->second;
+    return BSG_OK;
+  }
+  cudaGraph_t graph = nullptr;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaSuccess;
+  for (int64_t s = 0; s < nsw && e == cudaSuccess; ++s) e = enqueue_sweep(ctx, ctx->stream);
+  cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return fail(ctx, BSG_ERR_CUDA,
+                std::string("graph capture: ") +
+                    cudaGetErrorString(e != cudaSuccess ? e : e2));
+  }
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  CK(e);
+  ctx->graphs[nsw] = exec;
+  *out = exec;
+  return BSG_OK;
+}
+
+bool valid_chain(const bsg_ctx *ctx, int32_t c) {
+  return ctx && c >= 0 && c < (int32_t)ctx->ch.size();
+}
+
+
+ChainCounters *counters_of(const Chain &c) {
+  return reinterpret_cast<ChainCounters *>(c.dev.sweep);
+}
+
+}  // namespace
+
+// ========================================================================
+extern "C" {
+
+const char *bsg_status_string(bsg_status s) {
+  switch (s) {
+    case BSG_OK: return "ok";
+    case BSG_ERR_INVALID: return "invalid argument";
+    case BSG_ERR_CUDA: return "CUDA error";
+    case BSG_ERR_NOT_SPD: return "matrix not positive definite";
+    case BSG_ERR_SAMPLER_CAP: return "sampler iteration cap reached";
+    case BSG_ERR_NAN: return "non-finite sampler state";
+    case BSG_ERR_STATE: return "call out of order";
+    case BSG_ERR_NO_DEVICE: return "no CUDA device";
+    case BSG_ERR_UNSUPPORTED: return "unsupported size";
+    default: return "unknown status";
+  }
+}
+
+const char *bsg_last_error(const bsg_ctx *ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+bsg_status bsg_create(int32_t device, bsg_ctx **out) {
+  if (!out) return BSG_ERR_INVALID;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return BSG_ERR_NO_DEVICE;
+  if (device < 0 || device >= n) return BSG_ERR_INVALID;
+  std::unique_ptr<bsg_ctx> c(new bsg_ctx());
+  bsg_ctx *ctx = c.get();
+  ctx->device = device;
+  CK(cudaSetDevice(device));
+  CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming));
+  *out = c.release();
+  return BSG_OK;
+}
+
+bsg_status bsg_destroy(bsg_ctx *ctx) {
+  if (!ctx) return BSG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  clear_graphs(ctx);
+  for (auto &b : ctx->owned) cudaFree(b.p);
+  for (auto s : ctx->side) cudaStreamDestroy(s);
+  for (auto e : ctx->join) cudaEventDestroy(e);
+  if (ctx->fork) cudaEventDestroy(ctx->fork);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return BSG_OK;
+}
+
+bsg_status bsg_add_dataset(bsg_ctx *ctx, const bsg_dataset_desc *desc,
+                           int32_t *dataset_id) {
+  if (!ctx || !desc || !dataset_id) return BSG_ERR_INVALID;
+  const bsg_dataset_desc &q = *desc;
+  if (q.nrow < 1 || q.ncol < 1 || q.ndepth < 1 || !q.mask || !q.covar || !q.data)
+    return fail(ctx, BSG_ERR_INVALID, "dataset: empty grid or null input");
+  const double padded = (double)(q.nrow + 2) * (q.ncol + 2) * (q.ndepth + 2);
+  if (padded > 2.0e9) return fail(ctx, BSG_ERR_UNSUPPORTED, "grid too large");
+  if (q.ncovar < 1 || q.ncovar > BSG_MAX_COVAR)
+    return fail(ctx, BSG_ERR_UNSUPPORTED, "ncovar must be in 1..8");
+  if (q.nsubtypes < 0 || q.nsubtypes > q.ncovar)
+    return fail(ctx, BSG_ERR_INVALID, "nsubtypes must be in 0..ncovar");
+  if (q.nsubs < 1 || q.nsubs > (1 << 26))
+    return fail(ctx, BSG_ERR_INVALID, "nsubs out of range");
+  CK(cudaSetDevice(ctx->device));
+  Dataset d;
+  d.X = q.nrow;
+  d.Y = q.ncol;
+  d.Z = q.ndepth;
+  d.N = q.nsubs;
+  d.P = q.ncovar;
+  d.S = q.nsubtypes;
+  build_lattice(d, q.mask);
+  if (d.V == 0) return fail(ctx, BSG_ERR_INVALID, "mask is empty");
+  if ((double)d.N * d.V > 4.0e12)
+    return fail(ctx, BSG_ERR_UNSUPPORTED, "N*V too large");
+  // X'X in float, subject order (read_data.cpp:321-327).
+  std::vector<float> xtx((size_t)d.P * d.P, 0.f);
+  for (int i = 0; i < d.N; ++i)
+    for (int a = 0; a < d.P; ++a)
+      for (int b = 0; b < d.P; ++b)
+        xtx[b + a * d.P] += q.covar[(size_t)a * d.N + i] * q.covar[(size_t)b * d.N + i];
+  cudaError_t e;
+  DatasetDev &dv = d.dev;
+  dv.N = d.N;
+  dv.P = d.P;
+  dv.S = d.S;
+  dv.V = d.V;
+  dv.Vp = d.Vp;
+  dv.W = (d.N + 31) / 32;
+  dv.covar = upload(ctx, q.covar, (size_t)d.P * d.N, &e);
+  CK(e);
+  dv.xtx = upload(ctx, xtx.data(), xtx.size(), &e);
+  CK(e);
+  dv.wm = nullptr;
+  if (q.wm) {
+    dv.wm = upload(ctx, q.wm, (size_t)d.V, &e);
+    CK(e);
+  }
+  uint8_t *bytes = upload(ctx, q.data, (size_t)d.N * d.V, &e);
+  CK(e);
+  int *status = (int *)dalloc(ctx, sizeof(int), &e);
+  CK(e);
+  CK(cudaMemset(status, 0, sizeof(int)));
+  const int sy = d.PX, sz = d.PX * d.PY;
+  const int off[6] = {-1, 1, -sy, sy, -sz, sz};
+  for (int c = 0; c < 2; ++c) {
+    const int nc = (int)d.vox[c].size();
+    dv.n[c] = nc;
+    std::vector<int32_t> nb((size_t)7 * nc), vi(nc);
+    for (int j = 0; j < nc; ++j) {
+      const int p = d.vox[c][j];
+      nb[j] = d.idxsc[p];
+      for (int t = 0; t < 6; ++t) nb[(size_t)(t + 1) * nc + j] = d.idxsc[p + off[t]];
+      vi[j] = d.idx[p];
+    }
+    dv.nb[c] = upload(ctx, nb.data(), nb.size(), &e);
+    CK(e);
+    dv.nnb[c] = upload(ctx, d.nbrs[c].data(), d.nbrs[c].size(), &e);
+    CK(e);
+    dv.vidx[c] = upload(ctx, vi.data(), vi.size(), &e);
+    CK(e);
+    uint32_t *yb = (uint32_t *)dalloc(ctx, sizeof(uint32_t) * (size_t)dv.W * nc, &e);
+    CK(e);
+    dv.ybits[c] = yb;
+    CK(launch_pack(bytes, d.N, d.V, nc, dv.vidx[c], yb, status, ctx->stream));
+  }
+  int bad = 0;
+  CK(cudaMemcpyAsync(&bad, status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  dfree(ctx, bytes);
+  dfree(ctx, status);
+  if (bad) return fail(ctx, BSG_ERR_INVALID, "outcome values must be 0 or 1");
+  ctx->ds.push_back(std::move(d));
+  *dataset_id = (int32_t)ctx->ds.size() - 1;
+  ctx->plan_valid = false;
+  return BSG_OK;
+}
+
+bsg_status bsg_add_chain(bsg_ctx *ctx, int32_t dataset_id,
+                         const bsg_chain_desc *desc, int32_t *chain_id) {
+  if (!ctx || !desc || !chain_id) return BSG_ERR_INVALID;
+  if (dataset_id < 0 || dataset_id >= (int32_t)ctx->ds.size())
+    return fail(ctx, BSG_ERR_INVALID, "no such dataset");
+  if (desc->thin < 1) return fail(ctx, BSG_ERR_INVALID, "thin must be >= 1");
+  if (ctx->ch.size() >= (1u << 23))
+    return fail(ctx, BSG_ERR_UNSUPPORTED, "too many chains");
+  const Dataset &d = ctx->ds[dataset_id];
+  if ((double)d.V + desc->df_offset < d.P)
+    return fail(ctx, BSG_ERR_INVALID, "Wishart df = V + df_offset must be >= P");
+  CK(cudaSetDevice(ctx->device));
+  Chain c;
+  c.dataset = dataset_id;
+  c.desc = *desc;
+  ChainDev &cv = c.dev;
+  cudaError_t e;
+  cv.dataset = dataset_id;
+  cv.key0 = (uint32_t)(desc->seed & 0xFFFFFFFFu);
+  cv.key1 = (uint32_t)(desc->seed >> 32);
+  cv.chain_id = (uint32_t)ctx->ch.size();
+  cv.beta_wm = desc->beta_wm;
+  cv.df_offset = desc->df_offset;
+  cv.burnin = desc->burnin;
+  cv.thin = desc->thin;
+  const int per = kPostThreads * kPostPerThread;
+  cv.post_blocks = (d.V + per - 1) / per;
+  const int P = d.P;
+  cv.beta = (float *)dalloc(ctx, sizeof(float) * (size_t)P * d.Vp, &e);
+  CK(e);
+  CK(cudaMemset(cv.beta, 0, sizeof(float) * (size_t)P * d.Vp));
+  std::vector<double> eye((size_t)P * P, 0.0);
+  std::vector<float> eyef((size_t)P * P, 0.f);
+  for (int i = 0; i < P; ++i) eye[i + i * P] = 1.0, eyef[i + i * P] = 1.f;
+  cv.omega_d = upload(ctx, eye.data(), eye.size(), &e);
+  CK(e);
+  cv.omega_f = upload(ctx, eyef.data(), eyef.size(), &e);
+  CK(e);
+  cv.colmean = (float *)dalloc(ctx, sizeof(float) * P, &e);
+  CK(e);
+  CK(cudaMemset(cv.colmean, 0, sizeof(float) * P));
+  const size_t nacc = (size_t)P * d.V, nprb = (size_t)d.S * d.V;
+  cv.acc_mean = (double *)dalloc(ctx, sizeof(double) * nacc, &e);
+  CK(e);
+  cv.acc_m2 = (double *)dalloc(ctx, sizeof(double) * nacc, &e);
+  CK(e);
+  cv.acc_prb = (double *)dalloc(ctx, sizeof(double) * (nprb ? nprb : 1), &e);
+  CK(e);
+  CK(cudaMemset(cv.acc_mean, 0, sizeof(double) * nacc));
+  CK(cudaMemset(cv.acc_m2, 0, sizeof(double) * nacc));
+  if (nprb) CK(cudaMemset(cv.acc_prb, 0, sizeof(double) * nprb));
+  cv.partials = (double *)dalloc(ctx, sizeof(double) * (size_t)cv.post_blocks * kPostVals, &e);
+  CK(e);
+  ChainCounters *cnt = (ChainCounters *)dalloc(ctx, sizeof(ChainCounters), &e);
+  CK(e);
+  CK(cudaMemset(cnt, 0, sizeof(ChainCounters)));
+  cv.sweep = &cnt->sweep;
+  cv.nkept = &cnt->nkept;
+  cv.done = &cnt->done;
+  cv.status = &cnt->status;
+  ctx->ch.push_back(c);
+  *chain_id = (int32_t)ctx->ch.size() - 1;
+  ctx->plan_valid = false;
+  return BSG_OK;
+}
+
+bsg_status bsg_set_tuning(bsg_ctx *ctx, int32_t lanes_per_voxel,
+                          int32_t block_threads) {
+  if (!ctx) return BSG_ERR_INVALID;
+  const int lpv = lanes_per_voxel ? lanes_per_voxel : ctx->lpv;
+  const int thr = block_threads ? block_threads : ctx->threads;
+  if (!fused_supported(1, lpv, thr))
+    return fail(ctx, BSG_ERR_UNSUPPORTED,
+                "lanes_per_voxel in {1,2,4,8}, block_threads in {64,128,256}");
+  if (lpv != ctx->lpv || thr != ctx->threads) {
+    ctx->lpv = lpv;
+    ctx->threads = thr;
+    ctx->plan_valid = false;
+  }
+  return BSG_OK;
+}
+
+bsg_status bsg_get_tuning(const bsg_ctx *ctx, int32_t *lpv, int32_t *thr) {
+  if (!ctx) return BSG_ERR_INVALID;
+  if (lpv) *lpv = ctx->lpv;
+  if (thr) *thr = ctx->threads;
+  return BSG_OK;
+}
+
+bsg_status bsg_run(bsg_ctx *ctx, int64_t nsweeps) {
+  if (!ctx || nsweeps < 0) return BSG_ERR_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  bsg_status s = build_plan(ctx);
+  if (s) return s;
+  int64_t left = nsweeps;
+  while (left > 0) {
+    int64_t seg = 64;
+    while (seg > left) seg >>= 1;
+    cudaGraphExec_t g;
+    if ((s = get_graph(ctx, seg, &g))) return s;
+    CK(cudaGraphLaunch(g, ctx->stream));
+    left -= seg;
+  }
+  return BSG_OK;
+}
+
+bsg_status bsg_sync(bsg_ctx *ctx) {
+  if (!ctx) return BSG_ERR_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  int bits = 0;
+  for (auto &c : ctx->ch) {
+    int b = 0;
+    CK(cudaMemcpy(&b, c.dev.status, sizeof(int), cudaMemcpyDeviceToHost));
+    bits |= b;
+  }
+  if (bits) {
+    ctx->err = "sampler:" + status_text(bits);
+    return status_from_bits(bits);
+  }
+  return BSG_OK;
+}
+
+bsg_status bsg_run_timed(bsg_ctx *ctx, int64_t nsweeps, double *ms) {
+  if (!ctx || !ms) return BSG_ERR_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  bsg_status s = build_plan(ctx);
+  if (s) return s;
+  // Warm the graph cache outside the timed region.
+  int64_t left = nsweeps;
+  while (left > 0) {
+    int64_t seg = 64;
+    while (seg > left) seg >>= 1;
+    cudaGraphExec_t g;
+    if ((s = get_graph(ctx, seg, &g))) return s;
+    left -= seg;
+  }
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  CK(cudaEventRecord(a, ctx->stream));
+  s = bsg_run(ctx, nsweeps);
+  CK(cudaEventRecord(b, ctx->stream));
+  CK(cudaEventSynchronize(b));
+  float f = 0.f;
+  CK(cudaEventElapsedTime(&f, a, b));
+  *ms = f;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return s;
+}
+
+bsg_status bsg_profile(bsg_ctx *ctx, int64_t nsweeps, double *ms,
+                       int64_t *launches) {
+  if (!ctx || !ms || nsweeps < 0) return BSG_ERR_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  bsg_status s = build_plan(ctx);
+  if (s) return s;
+  std::vector<cudaEvent_t> ev((size_t)3 * nsweeps);
+  for (auto &e : ev) CK(cudaEventCreate(&e));
+  const Supplied sup{};
+  int64_t nl[3] = {0, 0, 0};
+  for (int64_t i = 0; i < nsweeps; ++i) {
+    CK(cudaEventRecord(ev[3 * i], ctx->stream));
+    for (const Group &g : ctx->groups)
+      for (int c = 0; c < 2; ++c) {
+        CK(launch_fused(g.P, ctx->lpv, ctx->threads, false, ctx->d_ds, ctx->d_ch,
+                        g.d_map[c], (int)g.map[c].size(), c, sup, ctx->stream));
+        nl[0]++;
+      }
+    CK(cudaEventRecord(ev[3 * i + 1], ctx->stream));
+    CK(launch_post(ctx->d_ds, ctx->d_ch, ctx->d_post_map, ctx->post_blocks,
+                   false, sup, ctx->stream));
+    nl[1]++;
+    nl[2]++;
+    CK(cudaEventRecord(ev[3 * i + 2], ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  double t[3] = {0, 0, 0};
+  for (int64_t i = 0; i < nsweeps; ++i) {
+    float a = 0, b = 0, c = 0;
+    CK(cudaEventElapsedTime(&a, ev[3 * i], ev[3 * i + 1]));
+    CK(cudaEventElapsedTime(&b, ev[3 * i + 1], ev[3 * i + 2]));
+    CK(cudaEventElapsedTime(&c, ev[3 * i], ev[3 * i + 2]));
+    t[0] += a;
+    t[1] += b;
+    t[2] += c;
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  for (int i = 0; i < 3; ++i) {
+    ms[i] = t[i];
+    if (launches) launches[i] = nl[i];
+  }
+  return BSG_OK;
+}
+
+int64_t bsg_launches_per_sweep(const bsg_ctx *ctx) {
+  if (!ctx) return 0;
+  size_t ng = 0;
+  std::vector<int> ps;
+  for (auto &c : ctx->ch) {
+    const int P = ctx->ds[c.dataset].P;
+    if (std::find(ps.begin(), ps.end(), P) == ps.end()) ps.push_back(P);
+  }
+  ng = ps.size();
+  return (int64_t)(2 * ng + 1);
+}
+
+void *bsg_stream(bsg_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+bsg_status bsg_dataset_info(const bsg_ctx *ctx, int32_t id, int64_t *info) {
+  if (!ctx || !info || id < 0 || id >= (int32_t)ctx->ds.size()) return BSG_ERR_INVALID;
+  const Dataset &d = ctx->ds[id];
+  const int64_t v[11] = {d.X, d.Y, d.Z, d.nsize, d.V, d.Vp,
+                         (int64_t)d.vox[0].size(), (int64_t)d.vox[1].size(),
+                         d.N, d.P, d.S};
+  std::memcpy(info, v, sizeof(v));
+  return BSG_OK;
+}
+
+bsg_status bsg_get_lattice(const bsg_ctx *ctx, int32_t id, int32_t *idx,
+                           int32_t *idxsc, int32_t *vox0, int32_t *vox1,
+                           uint8_t *nbrs0, uint8_t *nbrs1) {
+  if (!ctx || id < 0 || id >= (int32_t)ctx->ds.size()) return BSG_ERR_INVALID;
+  const Dataset &d = ctx->ds[id];
+  if (idx) std::memcpy(idx, d.idx.data(), sizeof(int32_t) * d.nsize);
+  if (idxsc) std::memcpy(idxsc, d.idxsc.data(), sizeof(int32_t) * d.nsize);
+  if (vox0) std::memcpy(vox0, d.vox[0].data(), sizeof(int32_t) * d.vox[0].size());
+  if (vox1) std::memcpy(vox1, d.vox[1].data(), sizeof(int32_t) * d.vox[1].size());
+  if (nbrs0) std::memcpy(nbrs0, d.nbrs[0].data(), d.nbrs[0].size());
+  if (nbrs1) std::memcpy(nbrs1, d.nbrs[1].data(), d.nbrs[1].size());
+  return BSG_OK;
+}
+
+bsg_status bsg_get_beta(bsg_ctx *ctx, int32_t chain, float *out) {
+  if (!valid_chain(ctx, chain) || !out) return BSG_ERR_INVALID;
+  const Chain &c = ctx->ch[chain];
+  const Dataset &d = ctx->ds[c.dataset];
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(out, c.dev.beta, sizeof(float) * (size_t)d.P * d.Vp, cudaMemcpyDeviceToHost));
+  return BSG_OK;
+}
+
+bsg_status bsg_set_beta(bsg_ctx *ctx, int32_t chain, const float *in) {
+  if (!valid_chain(ctx, chain) || !in) return BSG_ERR_INVALID;
+  const Chain &c = ctx->ch[chain];
+  const Dataset &d = ctx->ds[c.dataset];
+  // Entries outside the mask (the dilated border) must stay zero: they are
+  // the out-of-mask neighbours (covarGPU.cu:357-362).
+  std::vector<float> b(in, in + (size_t)d.P * d.Vp);
+  std::vector<char> inmask(d.Vp, 0);
+  for (int p = 0; p < d.nsize; ++p)
+    if (d.idx[p] >= 0) inmask[d.idxsc[p]] = 1;
+  for (int p = 0; p < d.P; ++p)
+    for (int s = 0; s < d.Vp; ++s)
+      if (!inmask[s]) b[(size_t)p * d.Vp + s] = 0.f;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(c.dev.beta, b.data(), sizeof(float) * b.size(), cudaMemcpyHostToDevice));
+  return BSG_OK;
+}
+
+bsg_status bsg_get_omega(bsg_ctx *ctx, int32_t chain, double *out) {
+  if (!valid_chain(ctx, chain) || !out) return BSG_ERR_INVALID;
+  const Chain &c = ctx->ch[chain];
+  const int P = ctx->ds[c.dataset].P;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(out, c.dev.omega_d, sizeof(double) * P * P, cudaMemcpyDeviceToHost));
+  return BSG_OK;
+}
+
+bsg_status bsg_set_omega(bsg_ctx *ctx, int32_t chain, const double *in) {
+  if (!valid_chain(ctx, chain) || !in) return BSG_ERR_INVALID;
+  const Chain &c = ctx->ch[chain];
+  const int P = ctx->ds[c.dataset].P;
+  std::vector<float> f(in, in + P * P);
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(c.dev.omega_d, in, sizeof(double) * P * P, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c.dev.omega_f, f.data(), sizeof(float) * P * P, cudaMemcpyHostToDevice));
+  return BSG_OK;
+}
+
+bsg_status bsg_get_colmeans(bsg_ctx *ctx, int32_t chain, float *out) {
+  if (!valid_chain(ctx, chain) || !out) return BSG_ERR_INVALID;
+  const Chain &c = ctx->ch[chain];
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(out, c.dev.colmean, sizeof(float) * ctx->ds[c.dataset].P,
+                cudaMemcpyDeviceToHost));
+  return BSG_OK;
+}
+
+bsg_status bsg_get_sweep(bsg_ctx *ctx, int32_t chain, int64_t *sweep, int64_t *nkept) {
+  if (!valid_chain(ctx, chain)) return BSG_ERR_INVALID;
+  ChainCounters h{};
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(&h, counters_of(ctx->ch[chain]), sizeof(h), cudaMemcpyDeviceToHost));
+  if (sweep) *sweep = h.sweep;
+  if (nkept) *nkept = h.nkept;
+  return BSG_OK;
+}
+
+bsg_status bsg_compute_prb(bsg_ctx *ctx, int32_t chain, float *prb) {
+  if (!valid_chain(ctx, chain) || !prb) return BSG_ERR_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  bsg_status s = build_plan(ctx);
+  if (s) return s;
+  const Chain &c = ctx->ch[chain];
+  const Dataset &d = ctx->ds[c.dataset];
+  const size_t n = (size_t)d.S * d.V;
+  if (!n) return BSG_OK;
+  cudaError_t e;
+  float *dp = (float *)dalloc(ctx, sizeof(float) * n, &e);
+  CK(e);
+  CK(launch_prb(ctx->d_ds, ctx->d_ch, chain, d.dev, dp, ctx->stream));
+  CK(cudaMemcpyAsync(prb, dp, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  dfree(ctx, dp);
+  return BSG_OK;
+}
+
+bsg_status bsg_get_posterior(bsg_ctx *ctx, int32_t chain, double *mean,
+                             double *var, double *prb, int64_t *nkept) {
+  if (!valid_chain(ctx, chain)) return BSG_ERR_INVALID;
+  const Chain &c = ctx->ch[chain];
+  const Dataset &d = ctx->ds[c.dataset];
+  int64_t nk = 0;
+  bsg_status s = bsg_get_sweep(ctx, chain, nullptr, &nk);
+  if (s) return s;
+  const size_t n = (size_t)d.P * d.V;
+  if (mean) CK(cudaMemcpy(mean, c.dev.acc_mean, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (var) {
+    CK(cudaMemcpy(var, c.dev.acc_m2, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    const double den = (double)(nk - 1);
+    for (size_t i = 0; i < n; ++i) var[i] /= den;
+  }
+  if (prb && d.S)
+    CK(cudaMemcpy(prb, c.dev.acc_prb, sizeof(double) * (size_t)d.S * d.V,
+                  cudaMemcpyDeviceToHost));
+  if (nkept) *nkept = nk;
+  return BSG_OK;
+}
+
+bsg_status bsg_get_maps(bsg_ctx *ctx, int32_t chain, double *spatcoef,
+                        double *spatcoef_var, double *standcoef, double *prb) {
+  if (!valid_chain(ctx, chain)) return BSG_ERR_INVALID;
+  const Chain &c = ctx->ch[chain];
+  const Dataset &d = ctx->ds[c.dataset];
+  const size_t n = (size_t)d.P * d.V;
+  std::vector<double> mean(n), var(n), pr((size_t)d.S * d.V + 1);
+  int64_t nk = 0;
+  bsg_status s = bsg_get_posterior(ctx, chain, mean.data(), var.data(), pr.data(), &nk);
+  if (s) return s;
+  const size_t R = (size_t)d.X * d.Y * d.Z;
+  const int sy = d.PX, sz = d.PX * d.PY;
+  auto grid_of = [&](int v) {
+    const int p = d.pad_of_v[v];
+    const int k = p / sz, rem = p - k * sz, j = rem / sy, i = rem - j * sy;
+    return (size_t)(i - 1) + (size_t)d.X * (j - 1) + (size_t)d.X * d.Y * (k - 1);
+  };
+  if (spatcoef) std::fill(spatcoef, spatcoef + (size_t)d.P * R, 0.0);
+  if (spatcoef_var) std::fill(spatcoef_var, spatcoef_var + (size_t)d.P * R, 0.0);
+  if (standcoef) std::fill(standcoef, standcoef + (size_t)d.P * R, 0.0);
+  if (prb) std::fill(prb, prb + (size_t)d.S * R, 0.0);
+  for (int v = 0; v < d.V; ++v) {
+    const size_t r = grid_of(v);
+    for (int p = 0; p < d.P; ++p) {
+      const double m = mean[(size_t)p * d.V + v], va = var[(size_t)p * d.V + v];
+      if (spatcoef) spatcoef[(size_t)p * R + r] = m;
+      if (spatcoef_var) spatcoef_var[(size_t)p * R + r] = va;
+      if (standcoef && va > 0) standcoef[(size_t)p * R + r] = m / std::sqrt(va);
+    }
+    if (prb)
+      for (int g = 0; g < d.S; ++g) prb[(size_t)g * R + r] = pr[(size_t)g * d.V + v];
+  }
+  return BSG_OK;
+}
+
+bsg_status bsg_reset_accumulators(bsg_ctx *ctx, int32_t chain) {
+  if (!valid_chain(ctx, chain)) return BSG_ERR_INVALID;
+  const Chain &c = ctx->ch[chain];
+  const Dataset &d = ctx->ds[c.dataset];
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const size_t n = (size_t)d.P * d.V;
+  CK(cudaMemset(c.dev.acc_mean, 0, sizeof(double) * n));
+  CK(cudaMemset(c.dev.acc_m2, 0, sizeof(double) * n));
+  if (d.S) CK(cudaMemset(c.dev.acc_prb, 0, sizeof(double) * (size_t)d.S * d.V));
+  CK(cudaMemset(c.dev.nkept, 0, sizeof(long long)));
+  return BSG_OK;
+}
+
+bsg_status bsg_sweep_supplied(bsg_ctx *ctx, int32_t chain, const uint32_t *ubits,
+                              const float *normals, const double *chi2,
+                              const double *wnorm, int32_t form) {
+  if (!valid_chain(ctx, chain) || !ubits || !normals || !chi2 || !wnorm)
+    return BSG_ERR_INVALID;
+  if (form != 0 && form != 1) return fail(ctx, BSG_ERR_INVALID, "form must be 0 or 1");
+  CK(cudaSetDevice(ctx->device));
+  bsg_status s = build_plan(ctx);
+  if (s) return s;
+  const Chain &c = ctx->ch[chain];
+  const Dataset &d = ctx->ds[c.dataset];
+  cudaError_t e;
+  const int P = d.P, nw = P * (P - 1) / 2;
+  Supplied sup{};
+  uint32_t *du = upload(ctx, ubits, (size_t)d.N * d.V, &e);
+  CK(e);
+  float *dn = upload(ctx, normals, (size_t)d.V * P, &e);
+  CK(e);
+  double *dc = upload(ctx, chi2, (size_t)P, &e);
+  CK(e);
+  double *dw = upload(ctx, wnorm, (size_t)(nw ? nw : 1), &e);
+  CK(e);
+  sup.ubits = du;
+  sup.normals = dn;
+  sup.chi2 = dc;
+  sup.wnorm = dw;
+  sup.form = form;
+  // Block maps for this chain alone, one lane per voxel.
+  const int thr = 128;
+  std::vector<BlockMap> m[2], pm;
+  for (int col = 0; col < 2; ++col)
+    for (int st = 0; st < (int)d.vox[col].size(); st += thr)
+      m[col].push_back({chain, st});
+  const int per = kPostThreads * kPostPerThread;
+  for (int st = 0; st < d.V; st += per) pm.push_back({chain, st});
+  BlockMap *dm0 = upload(ctx, m[0].data(), m[0].size(), &e);
+  CK(e);
+  BlockMap *dm1 = upload(ctx, m[1].data(), m[1].size(), &e);
+  CK(e);
+  BlockMap *dpm = upload(ctx, pm.data(), pm.size(), &e);
+  CK(e);
+  CK(launch_fused(P, 1, thr, true, ctx->d_ds, ctx->d_ch, dm0, (int)m[0].size(), 0, sup,
+                  ctx->stream));
+  CK(launch_fused(P, 1, thr, true, ctx->d_ds, ctx->d_ch, dm1, (int)m[1].size(), 1, sup,
+                  ctx->stream));
+  CK(launch_post(ctx->d_ds, ctx->d_ch, dpm, (int)pm.size(), true, sup, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (void *p : {(void *)du, (void *)dn, (void *)dc, (void *)dw, (void *)dm0,
+                  (void *)dm1, (void *)dpm})
+    dfree(ctx, p);
+  return bsg_sync(ctx);
+}
+
+}  // extern "C"

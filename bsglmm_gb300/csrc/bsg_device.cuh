@@ -1,0 +1,173 @@
+// bsg_device.cuh -- device building blocks of the sampler: the Philox
+// counter-based generator, the canonical uniform / normal / truncated-normal
+// maps, register-resident Cholesky for P <= 8, and the A&S normal CDF.
+#pragma once
+
+#include <cstdint>
+
+#include "bsg_internal.h"
+
+namespace bsg {
+
+// ------------------------------------------------------------- Philox ----
+// Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): ten rounds of
+// (hi, lo) = M * x with M = 0xD2511F53 / 0xCD9E8D57 and Weyl key steps
+// 0x9E3779B9 / 0xBB67AE85.  Stateless: every variate of the sampler is a
+// pure function of (counter, key), so results do not depend on the launch
+// shape and resuming from a checkpoint is exact.
+struct PhiloxKey {
+  uint32_t k0[10], k1[10];  // round keys, precomputed once per thread
+  __device__ __forceinline__ void init(uint32_t a, uint32_t b) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+      k0[r] = a + (uint32_t)r * 0x9E3779B9u;
+      k1[r] = b + (uint32_t)r * 0xBB67AE85u;
+    }
+  }
+};
+
+__device__ __forceinline__ uint4 philox(uint4 c, const PhiloxKey &k) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.k0[r], lo1, hi0 ^ c.w ^ k.k1[r], lo0);
+  }
+  return c;
+}
+
+__device__ __forceinline__ uint4 philox1(uint4 c, uint32_t a, uint32_t b) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ a, lo1, hi0 ^ c.w ^ b, lo0);
+    a += 0x9E3779B9u;
+    b += 0xBB67AE85u;
+  }
+  return c;
+}
+
+__device__ __forceinline__ uint32_t pick4(uint4 r, int q) {
+  return q == 0 ? r.x : q == 1 ? r.y : q == 2 ? r.z : r.w;
+}
+
+// ------------------------------------------------ canonical variate maps --
+// u(k) = (k + 1/2) 2^-32 and 1 - u(k) = u(~k) are both formed from the
+// integer, so each tail keeps full relative precision.
+__device__ __forceinline__ float u_of(uint32_t k) {
+  return fmaf((float)k, 0x1p-32f, 0x1p-33f);
+}
+__device__ __forceinline__ double u_of_d(uint32_t k) {
+  return ((double)k + 0.5) * 0x1p-32;
+}
+
+// Standard normal by inversion with exact tails.
+__device__ __forceinline__ float normal_of(uint32_t k) {
+  const bool lo = k < 0x80000000u;
+  const float t = normcdfinvf(u_of(lo ? k : ~k));
+  return lo ? t : -t;
+}
+
+// N(0,1) truncated to (a, +inf) by inversion of u(k):
+//   t = Phi^-1(Phi(a) + u Q(a)),  evaluated as -Phi^-1(Q(a) (1-u)) once the
+// argument passes 1/2, so both tails keep relative precision.
+__device__ __forceinline__ float tn_lower_inv(float a, uint32_t k) {
+  const float T = normcdff(-fabsf(a));  // mass beyond |a|
+  const float Pa = a < 0.f ? T : 1.f - T;
+  const float Qa = a < 0.f ? 1.f - T : T;
+  const float pl = fmaf(u_of(k), Qa, Pa);
+  const bool lo = pl < 0.5f;
+  const float t = normcdfinvf(lo ? pl : Qa * u_of(~k));
+  return lo ? t : -t;
+}
+
+// Far tail a > kATail: Robert (1995) exponential proposal with rate
+// alpha* = (a + sqrt(a^2+4))/2, accept with prob exp(-(x - alpha*)^2/2).
+// Attempt t uses the pair (2(t&1), 2(t&1)+1) of the counter
+// (i*8 + t/2, v, sweep, chain<<8 | ZTAIL).  Bounded: on the cap it returns
+// a and clears *ok.
+static __device__ __noinline__ float tn_lower_tail(float a, uint32_t i, uint32_t v,
+                                            uint32_t sweep, uint32_t c3,
+                                            uint32_t key0, uint32_t key1,
+                                            int *ok) {
+  const float as = 0.5f * (a + sqrtf(fmaf(a, a, 4.f)));
+  for (int q = 0; q < kTailMax / 2; ++q) {
+    const uint4 r = philox1(make_uint4(i * 8u + (uint32_t)q, v, sweep, c3),
+                            key0, key1);
+    float x = a - logf(u_of(r.x)) / as, d = x - as;
+    if (logf(u_of(r.y)) < -0.5f * d * d) return x;
+    x = a - logf(u_of(r.z)) / as;
+    d = x - as;
+    if (logf(u_of(r.w)) < -0.5f * d * d) return x;
+  }
+  *ok = 0;
+  return a;
+}
+
+// Abramowitz & Stegun 26.2.17 normal CDF (covarGPU.cu:1672-1693 uses the
+// same published polynomial).
+__device__ __forceinline__ float prob_sdnorm(float x) {
+  const float b1 = 0.319381530f, b2 = -0.356563782f, b3 = 1.781477937f;
+  const float b4 = -1.821255978f, b5 = 1.330274429f, p = 0.2316419f;
+  const float c = 0.39894228f;
+  const float ax = fabsf(x);
+  const float t = 1.0f / (1.0f + p * ax);
+  const float tail =
+      c * expf(-x * x / 2.0f) * t *
+      (t * (t * (t * (t * b5 + b4) + b3) + b2) + b1);
+  return x >= 0.0f ? 1.0f - tail : tail;
+}
+
+// ----------------------------------------- packed lower-triangular algebra
+__host__ __device__ constexpr int tri(int r, int c) { return r * (r + 1) / 2 + c; }
+
+// Outer-product Cholesky in place on packed lower storage (the scheme of
+// cholesky.cpp:13-33, with divisions as there).  Returns false if a pivot
+// is not positive.
+template <int P, typename T>
+__device__ __forceinline__ bool chol_packed(T (&A)[P * (P + 1) / 2]) {
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < P; ++k) {
+    T d = A[tri(k, k)];
+    ok = ok && (d > T(0));
+    d = sqrt(d);
+    A[tri(k, k)] = d;
+#pragma unroll
+    for (int j = k + 1; j < P; ++j) A[tri(j, k)] = A[tri(j, k)] / d;
+#pragma unroll
+    for (int j = k + 1; j < P; ++j)
+#pragma unroll
+      for (int i = j; i < P; ++i) A[tri(i, j)] -= A[tri(i, k)] * A[tri(j, k)];
+  }
+  return ok;
+}
+
+// x := G^-1 x (forward substitution).
+template <int P, typename T>
+__device__ __forceinline__ void solve_lower(const T (&G)[P * (P + 1) / 2],
+                                            T (&x)[P]) {
+#pragma unroll
+  for (int a = 0; a < P; ++a) {
+    T s = T(0);
+#pragma unroll
+    for (int q = 0; q < a; ++q) s += G[tri(a, q)] * x[q];
+    x[a] = (x[a] - s) / G[tri(a, a)];
+  }
+}
+
+// x := G^-T x (back substitution).
+template <int P, typename T>
+__device__ __forceinline__ void solve_upper(const T (&G)[P * (P + 1) / 2],
+                                            T (&x)[P]) {
+#pragma unroll
+  for (int a = P - 1; a >= 0; --a) {
+    T s = T(0);
+#pragma unroll
+    for (int q = a + 1; q < P; ++q) s += G[tri(q, a)] * x[q];
+    x[a] = (x[a] - s) / G[tri(a, a)];
+  }
+}
+
+}  // namespace bsg

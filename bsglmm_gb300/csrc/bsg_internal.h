@@ -1,0 +1,105 @@
+// bsg_internal.h -- device-side descriptors shared by the kernels and the
+// host engine of libbsglmm_gb300.so.  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace bsg {
+
+constexpr int kMaxP = 8;                            // covariates per chain
+constexpr int kMaxPairs = kMaxP * (kMaxP + 1) / 2;  // lower-triangle pairs
+constexpr int kPostVals = kMaxPairs + kMaxP;        // pairs + column sums
+constexpr int kChunk = 512;                         // subjects staged per pass
+constexpr int kChunkPad = kChunk + kChunk / 32;     // one pad word per 32
+constexpr float kATail = 5.0f;  // inversion below, rejection above
+constexpr int kTailMax = 16;    // rejection attempts per latent draw
+constexpr int kGammaMax = 64;   // Marsaglia-Tsang attempts per gamma draw
+constexpr int kPostThreads = 256;
+constexpr int kPostPerThread = 4;
+
+// Philox counter tags: c3 = chain << 8 | tag.
+enum : uint32_t {
+  kTagZ = 1,
+  kTagZTail = 2,
+  kTagBeta = 3,
+  kTagWNorm = 4,
+  kTagGamma = 5,
+};
+
+// Sticky per-chain error bits (ChainDev::status).
+enum : int {
+  kErrTnCap = 1,
+  kErrChol = 2,
+  kErrNaN = 4,
+  kErrGammaCap = 8,
+  kErrWishart = 16,
+  kErrInput = 32,
+};
+
+// Read-only study data on the device.
+struct DatasetDev {
+  int32_t N, P, S, V, Vp, W;   // W = ceil(N / 32) outcome words per voxel
+  int32_t n[2];                // voxels per colour
+  const float *covar;          // [P][N]
+  const float *xtx;            // [P][P]  X'X in float (read_data.cpp:321)
+  const float *wm;             // [V] or nullptr (WM = 1)
+  const int32_t *nb[2];        // [7][n_c]: sc(self), sc of the 6 neighbours
+                               // in the order -x, +x, -y, +y, -z, +z
+  const uint8_t *nnb[2];       // [n_c] in-mask neighbour count
+  const int32_t *vidx[2];      // [n_c] compact mask index
+  const uint32_t *ybits[2];    // [W][n_c] outcome bits, bit b = subject 32w+b
+};
+
+// Sampler state of one chain on the device.
+struct ChainDev {
+  int32_t dataset;
+  uint32_t key0, key1, chain_id;
+  float beta_wm;
+  int32_t df_offset, burnin, thin;
+  int32_t post_blocks;     // blocks of the post-sweep kernel for this chain
+  float *beta;             // [P][Vp]
+  float *omega_f;          // [P*P] float copy read by the colour kernels
+  double *omega_d;         // [P*P]
+  float *colmean;          // [P]
+  double *acc_mean;        // [P][V]
+  double *acc_m2;          // [P][V]
+  double *acc_prb;         // [S][V]
+  double *partials;        // [post_blocks][kPostVals]
+  unsigned int *done;      // arrival counter of the post-sweep kernel
+  long long *sweep;        // index of the sweep being drawn
+  long long *nkept;        // kept sweeps accumulated
+  int *status;             // sticky error bits
+};
+
+// Parity mode: variates supplied by the caller instead of Philox.
+struct Supplied {
+  const uint32_t *ubits;   // [N][V]
+  const float *normals;    // [V][P]
+  const double *chi2;      // [P]
+  const double *wnorm;     // [P(P-1)/2]
+  int form;                // 0 reference draw, 1 production draw
+};
+
+struct BlockMap {
+  int32_t chain;
+  int32_t start;  // first colour position (fused) or merged position (post)
+};
+
+// ---- launchers (bsg_kernels.cu) ----------------------------------------
+cudaError_t launch_fused(int P, int lpv, int threads, bool supplied,
+                         const DatasetDev *ds, ChainDev *ch,
+                         const BlockMap *map, int nblocks, int colour,
+                         const Supplied &sup, cudaStream_t st);
+cudaError_t launch_post(const DatasetDev *ds, ChainDev *ch,
+                        const BlockMap *map, int nblocks, bool supplied,
+                        const Supplied &sup, cudaStream_t st);
+cudaError_t launch_prb(const DatasetDev *ds, const ChainDev *ch, int chain,
+                       const DatasetDev &dh, float *prb, cudaStream_t st);
+cudaError_t launch_pack(const uint8_t *bytes, int N, int V, int nc,
+                        const int32_t *vidx, uint32_t *ybits, int *status,
+                        cudaStream_t st);
+bool fused_supported(int P, int lpv, int threads);
+
+}  // namespace bsg

@@ -1,0 +1,160 @@
+/*
+ * bsglmm_gb300.h -- C ABI of libbsglmm_gb300.so, a GB300 (sm_103a) Gibbs
+ * sampler for the Bayesian spatial probit GLMM of BSGLMM.
+ *
+ * The reference (nicholst/BSGLMM) has no plugin layer: mcmc() calls the
+ * launchers of covarGPU.cu through prototypes declared in mcmc.cpp:101-125
+ * and shares state through extern globals.  This header is the native API
+ * that replaces those launchers; bsglmm_gb300/csrc/shim/covarGPU_shim.cpp
+ * maps the reference's own launcher signatures onto it.
+ *
+ * One context owns a CUDA stream and all device memory.  A context holds
+ * datasets (a mask lattice, a design matrix and binary outcome maps) and
+ * chains (sampler state over one dataset).  Every chain of a context is
+ * advanced by one batched launch sequence per sweep; bsg_run() replays
+ * CUDA-graph segments of sweeps.  Calls are asynchronous until a bsg_get_*
+ * or bsg_sync(); errors are returned as bsg_status, never by exit/assert.
+ *
+ * Array layouts are the reference's:
+ *   mask      X*Y*Z bytes, x fastest (NIfTI order, read_data.cpp:231-240)
+ *   covar     [P][N] floats, column-major   (read_data.cpp:302)
+ *   data      [N][V] bytes 0/1 by compact mask index (read_data.cpp:385)
+ *   spatcoef  [P][Vp] floats by compact dilated-mask index
+ *                                            (mcmc.cpp:227, main.cu:308-329)
+ *   omega     [P][P] precision of the MCAR prior, element (i,j) at j + i*P
+ *   maps      [P][X*Y*Z] doubles, x fastest  (mcmc.cpp:871-964)
+ */
+#ifndef BSGLMM_GB300_H
+#define BSGLMM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t bsg_status;
+enum {
+  BSG_OK = 0,
+  BSG_ERR_INVALID = 1,      /* bad argument or size out of range */
+  BSG_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+  BSG_ERR_NOT_SPD = 3,      /* a Cholesky pivot was not positive */
+  BSG_ERR_SAMPLER_CAP = 4,  /* a bounded rejection loop hit its cap */
+  BSG_ERR_NAN = 5,          /* non-finite sampler state */
+  BSG_ERR_STATE = 6,        /* call out of order (e.g. no chain) */
+  BSG_ERR_NO_DEVICE = 7,    /* no CUDA device / driver */
+  BSG_ERR_UNSUPPORTED = 8   /* outside the sizes this build supports */
+};
+
+#define BSG_MAX_COVAR 8 /* P; the reference allows 20 (covarGPU.cu:65-68) */
+
+typedef struct bsg_ctx bsg_ctx;
+
+/* One lesion-map study: the inputs BinCar reads (main.cu:82-116). */
+typedef struct {
+  int32_t nrow, ncol, ndepth; /* X, Y, Z: NROW, NCOL, NDEPTH */
+  int32_t nsubs;              /* N: NSUBS */
+  int32_t ncovar;             /* P: NCOVAR, 1..BSG_MAX_COVAR */
+  int32_t nsubtypes;          /* S: NSUBTYPES, 0..P (group columns) */
+  const uint8_t *mask;        /* X*Y*Z bytes, nonzero = in mask */
+  const float *covar;         /* [P][N] */
+  const uint8_t *data;        /* [N][V] 0/1 (values > 1 are rejected) */
+  const float *wm;            /* [V] white-matter covariate or NULL (= 1) */
+} bsg_dataset_desc;
+
+/* Sampler settings of one chain. */
+typedef struct {
+  uint64_t seed;     /* Philox key; the chain id is part of every counter */
+  int32_t df_offset; /* Wishart df = V + df_offset.  Reference CPU path:
+                        P (covar.cpp:291); reference GPU path: 19
+                        (covarGPU.cu:1104). */
+  int32_t burnin;    /* sweep s is kept iff s > burnin && s % thin == 0 */
+  int32_t thin;      /* (mcmc.cpp:303-308,584); thin >= 1 */
+  float beta_wm;     /* fixed WM coefficient; 0 when WM is off */
+} bsg_chain_desc;
+
+/* ---------------------------------------------------------- lifecycle -- */
+bsg_status bsg_create(int32_t device, bsg_ctx **out);
+bsg_status bsg_destroy(bsg_ctx *ctx);
+const char *bsg_status_string(bsg_status s);
+/* Message of the last error on this context ("" if none). */
+const char *bsg_last_error(const bsg_ctx *ctx);
+
+/* Builds the lattice (main.cu:189-394) and uploads the study. */
+bsg_status bsg_add_dataset(bsg_ctx *ctx, const bsg_dataset_desc *desc,
+                           int32_t *dataset_id);
+/* Adds a chain with beta = 0 and Omega = I (mcmc.cpp:149-154,227). */
+bsg_status bsg_add_chain(bsg_ctx *ctx, int32_t dataset_id,
+                         const bsg_chain_desc *desc, int32_t *chain_id);
+/* Tile shape of the fused colour kernel: lanes per voxel (1,2,4,8,16,32)
+ * and threads per block (64..1024); 0 keeps the current choice. */
+bsg_status bsg_set_tuning(bsg_ctx *ctx, int32_t lanes_per_voxel,
+                          int32_t block_threads);
+bsg_status bsg_get_tuning(const bsg_ctx *ctx, int32_t *lanes_per_voxel,
+                          int32_t *block_threads);
+
+/* ------------------------------------------------------------ sampling -- */
+/* Advances every chain by nsweeps sweeps (one sweep = latent Z + beta for
+ * both colours, the Omega Wishart draw, and on kept sweeps the posterior
+ * accumulators).  Asynchronous. */
+bsg_status bsg_run(bsg_ctx *ctx, int64_t nsweeps);
+/* Waits for the context's stream; returns the first sampler error seen. */
+bsg_status bsg_sync(bsg_ctx *ctx);
+/* Runs nsweeps and reports elapsed device time (CUDA events on the
+ * context's stream around the whole batch). */
+bsg_status bsg_run_timed(bsg_ctx *ctx, int64_t nsweeps, double *ms);
+/* Runs nsweeps without graphs with CUDA events around each kernel class:
+ * ms[0] fused colour kernels, ms[1] Omega/accumulator pass (including the
+ * Wishart tail), ms[2] whole sweeps.  launches[0..2] counts. */
+bsg_status bsg_profile(bsg_ctx *ctx, int64_t nsweeps, double *ms,
+                       int64_t *launches);
+/* Kernel launches issued per sweep by bsg_run (for launch accounting). */
+int64_t bsg_launches_per_sweep(const bsg_ctx *ctx);
+/* The context's cudaStream_t, for callers that record their own events. */
+void *bsg_stream(bsg_ctx *ctx);
+
+/* ----------------------------------------------------------- state I/O -- */
+bsg_status bsg_dataset_info(const bsg_ctx *ctx, int32_t dataset_id,
+                            int64_t *info /* X,Y,Z,nsize,V,Vp,n0,n1,N,P,S */);
+bsg_status bsg_get_lattice(const bsg_ctx *ctx, int32_t dataset_id,
+                           int32_t *idx, int32_t *idxsc, int32_t *vox0,
+                           int32_t *vox1, uint8_t *nbrs0, uint8_t *nbrs1);
+bsg_status bsg_get_beta(bsg_ctx *ctx, int32_t chain, float *spatcoef);
+bsg_status bsg_set_beta(bsg_ctx *ctx, int32_t chain, const float *spatcoef);
+bsg_status bsg_get_omega(bsg_ctx *ctx, int32_t chain, double *omega);
+bsg_status bsg_set_omega(bsg_ctx *ctx, int32_t chain, const double *omega);
+/* Column means of the last sweep (covarGPU.cu:563-583). */
+bsg_status bsg_get_colmeans(bsg_ctx *ctx, int32_t chain, float *means);
+bsg_status bsg_get_sweep(bsg_ctx *ctx, int32_t chain, int64_t *sweep,
+                         int64_t *nkept);
+/* Lesion probability of the current state (compute_prbGPU,
+ * covarGPU.cu:1814-1824): prb[g*V + v], A&S 26.2.17. */
+bsg_status bsg_compute_prb(bsg_ctx *ctx, int32_t chain, float *prb);
+/* Posterior summaries by compact mask index: mean[p*V+v], var[p*V+v]
+ * (divisor nkept-1), prb[g*V+v]. */
+bsg_status bsg_get_posterior(bsg_ctx *ctx, int32_t chain, double *mean,
+                             double *var, double *prb, int64_t *nkept);
+/* The reference's output maps on the X*Y*Z grid, zero outside the mask
+ * (mcmc.cpp:871-964): spatCoef_*, spatCoef_*.Var, standCoef_*, prb_*.
+ * Any pointer may be NULL. */
+bsg_status bsg_get_maps(bsg_ctx *ctx, int32_t chain, double *spatcoef,
+                        double *spatcoef_var, double *standcoef, double *prb);
+/* Clears the posterior accumulators and the kept-sweep count. */
+bsg_status bsg_reset_accumulators(bsg_ctx *ctx, int32_t chain);
+
+/* ---------------------------------------------------- parity interface -- */
+/* One sweep of one chain driven by supplied variates instead of Philox:
+ * ubits [N][V] 32-bit uniforms for the latent draws (u = (k+1/2)/2^32,
+ * inverted through the truncated normal CDF), normals [V][P] for the beta
+ * draws, chi2[P] and wnorm[P(P-1)/2] for the Bartlett Wishart draw.
+ * form 0 draws beta = m + chol(Q^-1) e as covar.cpp:168-177 does; form 1
+ * draws beta = m + G^-T e with Q = G G' (the production form). */
+bsg_status bsg_sweep_supplied(bsg_ctx *ctx, int32_t chain,
+                              const uint32_t *ubits, const float *normals,
+                              const double *chi2, const double *wnorm,
+                              int32_t form);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,372 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes access to the oracle.
+
+* ``Problem`` wraps liboracle.so, the FP64 C restatement of the reference's
+  CPU sweep (bsg_oracle.c).
+* ``RefSupplied`` / ``RefKiss`` wrap oracle/_ref/, the reference's own
+  covar.cpp + cholesky.cpp (+ randgen.cpp) compiled from the reference tree,
+  driven by supplied variates or by its own KISS generator.  These exist
+  only where the reference tree was present at build time.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIBORACLE = HERE / "liboracle.so"
+REF_SUPPLIED = HERE / "_ref" / "libbsgref_supplied.so"
+REF_KISS = HERE / "_ref" / "libbsgref_kiss.so"
+
+_P = C.c_void_p
+_d = C.c_double
+_i = C.c_int
+_i64 = C.c_int64
+_u32 = C.c_uint32
+
+
+def build_oracle(ref: bool = False) -> None:
+    """make liboracle.so (and, if requested and possible, oracle/_ref)."""
+    subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
+    if ref:
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True)
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+_O = None
+
+
+def lib() -> C.CDLL:
+    global _O
+    if _O is None:
+        if not LIBORACLE.exists():
+            build_oracle()
+        L = C.CDLL(str(LIBORACLE))
+        sig = {
+            "orc_philox4x32_10": (None, [_P, _P, _P]),
+            "orc_philox_block": (None, [_u32, _u32, _u32, _u32, _u32, _i64, _P]),
+            "orc_u_from_bits": (_d, [_u32]),
+            "orc_ncdf": (_d, [_d]),
+            "orc_ndtri": (_d, [_d]),
+            "orc_normal_from_bits": (_d, [_u32]),
+            "orc_tn_lower_inv": (_d, [_d, _u32]),
+            "orc_tn_lower_tail": (_i, [_d, _P, _i, _P]),
+            "orc_problem_new": (_P, [_i, _i, _i, _P, _i, _i, _i, _P, _P, _P]),
+            "orc_problem_free": (None, [_P]),
+            "orc_problem_info": (None, [_P, _P]),
+            "orc_problem_lattice": (None, [_P, _P, _P, _P, _P, _P, _P]),
+            "orc_problem_xtx": (None, [_P, _P]),
+            "orc_update_z": (None, [_P, _d, _P, _P, _P]),
+            "orc_update_spatcoef": (_i, [_P, _d, _P, _P, _P, _i, _P]),
+            "orc_spatcoef_prec_S": (None, [_P, _P, _P]),
+            "orc_wishart_from_S": (_i, [_i, _P, _P, _P, _P]),
+            "orc_prob_sdnorm": (_d, [_d]),
+            "orc_compute_prb": (None, [_P, _d, _P, _P]),
+            "orc_col_means": (None, [_P, _P, _P]),
+            "orc_chain_run": (_i, [_P, _P, _i64, _i64, _P, _P, _P, _P, _P, _P]),
+            "orc_port_new": (_P, [_P, C.c_uint64, _i]),
+            "orc_port_free": (None, [_P]),
+            "orc_port_sweep": (None, [_P, _i]),
+            "orc_port_updates": (_i64, [_P, _i]),
+        }
+        for k, (r, a) in sig.items():
+            f = getattr(L, k)
+            f.restype = r
+            f.argtypes = a
+        _O = L
+    return _O
+
+
+class ChainCfg(C.Structure):
+    _fields_ = [("key0", C.c_uint32), ("key1", C.c_uint32), ("chain", C.c_uint32),
+                ("df_offset", C.c_int32), ("burnin", C.c_int32), ("thin", C.c_int32),
+                ("beta_wm", C.c_double)]
+
+
+def philox(ctr, key) -> np.ndarray:
+    c = np.asarray(ctr, dtype=np.uint32)
+    k = np.asarray(key, dtype=np.uint32)
+    o = np.zeros(4, np.uint32)
+    lib().orc_philox4x32_10(_p(c), _p(k), _p(o))
+    return o
+
+
+def philox_block(c1, c2, c3, key0, key1, n4) -> np.ndarray:
+    o = np.zeros(4 * n4, np.uint32)
+    lib().orc_philox_block(c1, c2, c3, key0, key1, n4, _p(o))
+    return o
+
+
+class Problem:
+    """An oracle problem: lattice + design + outcomes (+ WM)."""
+
+    def __init__(self, mask, covar, data, nsubtypes=1, wm=None):
+        self._L = lib()
+        self.mask = np.ascontiguousarray(mask, dtype=np.uint8)
+        self.covar = np.ascontiguousarray(covar, dtype=np.float32)
+        self.data = np.ascontiguousarray(data, dtype=np.uint8)
+        self.wm = None if wm is None else np.ascontiguousarray(wm, dtype=np.float32)
+        Z, Y, X = self.mask.shape
+        P, N = self.covar.shape
+        self.S = nsubtypes
+        self.h = self._L.orc_problem_new(X, Y, Z, _p(self.mask), N, P, nsubtypes,
+                                         _p(self.covar), _p(self.data), _p(self.wm))
+        info = np.zeros(10, np.int64)
+        self._L.orc_problem_info(self.h, _p(info))
+        (self.X, self.Y, self.Z, self.nsize, self.V, self.Vp, self.n0, self.n1,
+         self.N, self.P) = map(int, info)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self._L.orc_problem_free(self.h)
+            self.h = None
+
+    def lattice(self) -> dict:
+        idx = np.zeros(self.nsize, np.int32)
+        idxsc = np.zeros(self.nsize, np.int32)
+        v0 = np.zeros(self.n0, np.int32)
+        v1 = np.zeros(self.n1, np.int32)
+        b0 = np.zeros(self.n0, np.uint8)
+        b1 = np.zeros(self.n1, np.uint8)
+        self._L.orc_problem_lattice(self.h, _p(idx), _p(idxsc), _p(v0), _p(v1),
+                                    _p(b0), _p(b1))
+        return dict(idx=idx, idxsc=idxsc, vox=[v0, v1], nbrs=[b0, b1])
+
+    def xtx(self) -> np.ndarray:
+        o = np.zeros((self.P, self.P), np.float32)
+        self._L.orc_problem_xtx(self.h, _p(o))
+        return o
+
+    def update_z(self, spatcoef, ubits, beta_wm=0.0) -> np.ndarray:
+        b = np.ascontiguousarray(spatcoef, dtype=np.float64)
+        u = np.ascontiguousarray(ubits, dtype=np.uint32)
+        Z = np.zeros((self.N, self.V))
+        self._L.orc_update_z(self.h, beta_wm, _p(b), _p(u), _p(Z))
+        return Z
+
+    def update_spatcoef(self, spatcoef, Z, omega, normals, form=0, beta_wm=0.0):
+        b = np.array(spatcoef, dtype=np.float64, order="C")
+        z = np.ascontiguousarray(Z, dtype=np.float64)
+        om = np.ascontiguousarray(omega, dtype=np.float64)
+        e = np.ascontiguousarray(normals, dtype=np.float32)
+        fails = self._L.orc_update_spatcoef(self.h, beta_wm, _p(z), _p(om), _p(e),
+                                            form, _p(b))
+        return b, fails
+
+    def prec_S(self, spatcoef) -> np.ndarray:
+        b = np.ascontiguousarray(spatcoef, dtype=np.float64)
+        S = np.zeros((self.P, self.P))
+        self._L.orc_spatcoef_prec_S(self.h, _p(b), _p(S))
+        return S
+
+    def wishart(self, S, chi2, wnorm):
+        S = np.ascontiguousarray(S, dtype=np.float64)
+        c = np.ascontiguousarray(chi2, dtype=np.float64)
+        w = np.ascontiguousarray(wnorm, dtype=np.float64)
+        om = np.zeros((self.P, self.P))
+        ok = self._L.orc_wishart_from_S(self.P, _p(S), _p(c), _p(w), _p(om))
+        return om, bool(ok)
+
+    def compute_prb(self, spatcoef, beta_wm=0.0) -> np.ndarray:
+        b = np.ascontiguousarray(spatcoef, dtype=np.float64)
+        out = np.zeros((self.S, self.V))
+        self._L.orc_compute_prb(self.h, beta_wm, _p(b), _p(out))
+        return out
+
+    def col_means(self, spatcoef) -> np.ndarray:
+        b = np.ascontiguousarray(spatcoef, dtype=np.float64)
+        out = np.zeros(self.P)
+        self._L.orc_col_means(self.h, _p(b), _p(out))
+        return out
+
+    def sweep_supplied(self, spatcoef, omega, ubits, normals, chi2, wnorm,
+                       form=0, beta_wm=0.0):
+        """One full sweep (Z, beta both colours, Omega) from supplied
+        variates, in the reference's order; returns (beta, omega, Z)."""
+        Z = self.update_z(spatcoef, ubits, beta_wm)
+        b, fails = self.update_spatcoef(spatcoef, Z, omega, normals, form, beta_wm)
+        S = self.prec_S(b)
+        om, ok = self.wishart(S, chi2, wnorm)
+        return b, om, Z, S, fails, ok
+
+    def chain(self, seed: int, nsweeps: int, chain_id: int = 0, burnin: int = 0,
+              thin: int = 1, df_offset=None, beta_wm=0.0, s0: int = 0,
+              spatcoef=None, omega=None):
+        cfg = ChainCfg(seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF, chain_id,
+                       self.P if df_offset is None else df_offset, burnin, thin,
+                       beta_wm)
+        b = (np.zeros((self.P, self.Vp)) if spatcoef is None
+             else np.array(spatcoef, dtype=np.float64, order="C"))
+        om = np.eye(self.P) if omega is None else np.array(omega, dtype=np.float64, order="C")
+        mean = np.zeros((self.P, self.V))
+        m2 = np.zeros((self.P, self.V))
+        prb = np.zeros((max(self.S, 1), self.V))
+        nk = C.c_int64(0)
+        err = self._L.orc_chain_run(self.h, C.byref(cfg), s0, nsweeps, _p(b), _p(om),
+                                    _p(mean), _p(m2), _p(prb), C.byref(nk))
+        return dict(beta=b, omega=om, mean=mean, m2=m2, prb=prb[: self.S],
+                    nkept=nk.value, err=err)
+
+
+class Port:
+    """The CPU timing port of the reference sweep (float, KISS)."""
+
+    def __init__(self, problem: Problem, seed: int = 1, df_offset=None):
+        self._L = lib()
+        self.pb = problem
+        self.h = self._L.orc_port_new(problem.h, seed,
+                                      problem.P if df_offset is None else df_offset)
+
+    def sweep(self, nvox_limit: int = -1):
+        self._L.orc_port_sweep(self.h, nvox_limit)
+
+    def updates(self, nvox_limit: int = -1) -> int:
+        return int(self._L.orc_port_updates(self.h, nvox_limit))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self._L.orc_port_free(self.h)
+            self.h = None
+
+
+# ------------------------------------------------- the reference itself --
+class _Ref:
+    path: Path
+
+    def __init__(self, problem: Problem):
+        if not self.path.exists():
+            raise FileNotFoundError(f"{self.path} (build with `make -C oracle ref`)")
+        self._L = C.CDLL(str(self.path))
+        self.pb = problem
+        lat = problem.lattice()
+        self._keep = lat
+        L = self._L
+        L.ref_setup.argtypes = [_i] * 8 + [_P, _P, _i, _P, _P, _i, _P, _P, _P]
+        L.ref_setup(problem.X, problem.Y, problem.Z, problem.N, problem.P,
+                    problem.S, problem.V, problem.Vp, _p(lat["idx"]),
+                    _p(lat["idxsc"]), problem.n0, _p(lat["vox"][0]),
+                    _p(lat["nbrs"][0]), problem.n1, _p(lat["vox"][1]),
+                    _p(lat["nbrs"][1]), _p(problem.covar))
+        self.wm = (problem.wm if problem.wm is not None
+                   else np.ones(problem.V, np.float32))
+        for n, a in {"ref_update_z": [_P, _P, _P, C.c_float, _P, _P],
+                     "ref_update_spatcoef": [_P, _P, _P, _P, C.c_float, _P],
+                     "ref_update_spatcoef_prec": [_P, _P],
+                     "ref_compute_prb": [_P, _P, _P, C.c_float],
+                     "ref_xtx": [_P],
+                     "ref_cholesky_decomp": [_P, _i],
+                     "ref_cholesky_invert": [_P, _i]}.items():
+            getattr(L, n).argtypes = a
+        L.ref_prob_sdnorm.argtypes = [_d]
+        L.ref_prob_sdnorm.restype = _d
+        L.ref_cholesky_decomp.restype = _i
+
+    def xtx(self):
+        o = np.zeros((self.pb.P, self.pb.P), np.float32)
+        self._L.ref_xtx(_p(o))
+        return o
+
+    def update_z(self, spatcoef_f32, beta=0.0):
+        Z = np.zeros((self.pb.N, self.pb.V), np.float32)
+        b = np.ascontiguousarray(spatcoef_f32, dtype=np.float32)
+        self._L.ref_update_z(_p(Z), _p(self.pb.data), _p(self.wm), beta, _p(b),
+                             _p(self.pb.covar))
+        return Z
+
+    def update_spatcoef(self, spatcoef_f32, Z, omega_f32, beta=0.0):
+        b = np.array(spatcoef_f32, dtype=np.float32, order="C")
+        z = np.ascontiguousarray(Z, dtype=np.float32)
+        om = np.array(omega_f32, dtype=np.float32, order="C")
+        self._L.ref_update_spatcoef(_p(b), _p(z), _p(om), _p(self.wm), beta,
+                                    _p(self.pb.covar))
+        return b
+
+    def update_spatcoef_prec(self, spatcoef_f32):
+        om = np.zeros((self.pb.P, self.pb.P), np.float32)
+        b = np.ascontiguousarray(spatcoef_f32, dtype=np.float32)
+        self._L.ref_update_spatcoef_prec(_p(om), _p(b))
+        return om
+
+    def compute_prb(self, spatcoef_f32, beta=0.0):
+        out = np.zeros((self.pb.S, self.pb.V), np.float32)
+        b = np.ascontiguousarray(spatcoef_f32, dtype=np.float32)
+        self._L.ref_compute_prb(_p(out), _p(b), _p(self.wm), beta)
+        return out
+
+    def prob_sdnorm(self, x: float) -> float:
+        return self._L.ref_prob_sdnorm(x)
+
+
+class RefSupplied(_Ref):
+    path = REF_SUPPLIED
+
+    def __init__(self, problem: Problem):
+        super().__init__(problem)
+        L = self._L
+        L.ref_set_supplied.argtypes = [_P, _P, _P, _P]
+        L.ref_underrun.restype = _i
+        L.ref_gamma_shapes.argtypes = [_P, _i]
+        L.ref_gamma_shapes.restype = _i
+        L.ref_rwishart2.argtypes = [_P, _P, _i, _i, _P, _P]
+        L.ref_rwishart2.restype = _i
+
+    def set_supplied(self, ubits, normals, chi2, wnorm):
+        self._sup = [np.ascontiguousarray(ubits, dtype=np.uint32),
+                     np.ascontiguousarray(normals, dtype=np.float32),
+                     np.ascontiguousarray(chi2, dtype=np.float64),
+                     np.ascontiguousarray(wnorm if np.size(wnorm) else [0.0],
+                                          dtype=np.float64)]
+        self._L.ref_set_supplied(*[_p(a) for a in self._sup])
+
+    def underrun(self) -> bool:
+        return bool(self._L.ref_underrun())
+
+    def gamma_shapes(self):
+        o = np.zeros(64)
+        n = self._L.ref_gamma_shapes(_p(o), 64)
+        return o[:n]
+
+    def sweep(self, spatcoef_f32, omega_f32, beta=0.0):
+        """updateZ -> updateSpatCoef -> updateSpatCoefPrec
+        (mcmc.cpp:400,418,428) on the supplied variates."""
+        Z = self.update_z(spatcoef_f32, beta)
+        b = self.update_spatcoef(spatcoef_f32, Z, omega_f32, beta)
+        om = self.update_spatcoef_prec(b)
+        return b, om, Z
+
+
+class RefKiss(_Ref):
+    path = REF_KISS
+
+    def __init__(self, problem: Problem, seed=(1, 2, 3)):
+        super().__init__(problem)
+        L = self._L
+        L.ref_kiss_seed.argtypes = [C.c_uint64] * 3
+        L.ref_truncnorm_many.argtypes = [_d, _d, _d, _i, _P]
+        L.ref_snorm_many.argtypes = [_i, _P]
+        L.ref_rgamma_many.argtypes = [_d, _d, _i, _P]
+        L.ref_cpu_sweep.argtypes = [_P, _P, _P, _P, _P, _P]
+        L.ref_kiss_seed(*seed)
+
+    def truncnorm(self, mu, lo, hi, n):
+        out = np.zeros(n)
+        self._L.ref_truncnorm_many(mu, lo, hi, n, _p(out))
+        return out
+
+    def snorm(self, n):
+        out = np.zeros(n)
+        self._L.ref_snorm_many(n, _p(out))
+        return out
+
+    def rgamma(self, a, b, n):
+        out = np.zeros(n)
+        self._L.ref_rgamma_many(a, b, n, _p(out))
+        return out

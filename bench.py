@@ -1,0 +1,343 @@
+"""Benchmark of the GB300 probit Gibbs sampler.
+
+A step is one sweep of the sampler (latent Z + beta for both colours, the
+Omega Wishart draw, the posterior accumulators) over the brain-sized study:
+91x109x91 grid, ellipsoidal mask of about 230k voxels, N = 1000 subjects,
+P = 5 covariates, single chain, FP32 sweep with FP64 Omega/accumulators.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  `value` is subject*voxel updates per second with the
+study resident in HBM (device time of the K timed sweeps, L2 flushed between
+sweeps); `e2e` is the same metric through the C ABI with host buffers: each
+step uploads the chain's Omega from host memory (as the reference's
+updateSpatCoefGPU does, covarGPU.cu:540) and reads the new Omega and the
+column means back (covarGPU.cu:582,1106-1108).  With N > 1 (torchrun) every
+rank runs an independent chain on its own GPU (replicas, weak scaling).
+`--impl reference` times the reference's CPU sweep (the oracle's timing port
+of covar.cpp's updateZ / updateSpatCoef / updateSpatCoefPrec) on all host
+cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = ("subj·voxel updates/s & sweeps/s, batched-split vs plain GPU form, "
+          "≤0.5 MCSE err")
+UNIT = "subject-voxel updates/s"
+WORKLOAD = "brain-sized plain FP32 GPU form: 91x109x91 grid, ellipsoid mask, N=1000, P=5"
+C_TN = 40          # FP32 flops of one truncated-normal draw's accept path
+L2_FLUSH_BYTES = 512 << 20
+CPU_SAMPLE_VOX = 3000   # voxels per colour per thread in a CPU baseline step
+
+
+def fused_flops_per_update(P: int) -> int:
+    """Algorithmic FP32 flops per subject-voxel update: eta = x'beta and the
+    X'Z accumulation (2P each) plus the truncated-normal draw."""
+    return 4 * P + C_TN
+
+
+def sweep_bytes(N: int, V: int, P: int, S: int, kept: bool = True) -> int:
+    """Minimum HBM bytes of one sweep: outcome bits, beta read+write, the
+    Omega pass read of beta, FP64 accumulators (mean, M2, prb mean read and
+    write) and 5 B of lattice metadata per voxel."""
+    b = N * V // 8 + 8 * P * V + 4 * P * V + 5 * V
+    if kept:
+        b += 2 * 8 * (2 * P + S) * V
+    return b
+
+
+# ------------------------------------------------------------ utilities --
+def dist_env():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the
+    timed region runs."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": mx, "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {}
+
+
+# ------------------------------------------------------------ CPU legs ---
+def cpu_port_rate(study, threads: int, steps: int, warmup: int, nvox: int):
+    """The oracle's timing port of the reference CPU sweep, one independent
+    chain per thread, each step restricted to `nvox` voxels per colour."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    oracle.build_oracle()
+    pb = oracle.Problem(study.mask, study.covar, study.data, study.nsubtypes)
+    ports = [oracle.Port(pb, seed=1000 + t) for t in range(threads)]
+    upd = ports[0].updates(nvox)
+
+    def work(pt, n):
+        for _ in range(n):
+            pt.sweep(nvox)
+
+    def run(n):
+        ts = [threading.Thread(target=work, args=(pt, n)) for pt in ports]
+        t0 = time.perf_counter()
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        return time.perf_counter() - t0
+
+    if warmup:
+        run(warmup)
+    dt = run(steps)
+    rate = upd * threads * steps / dt
+    sample = (f"{steps} sweep(s) per thread restricted to the first {nvox} voxels "
+              f"of each colour ({upd} subject-voxel updates per sweep), "
+              f"{threads} independent chains")
+    return rate, dt / steps, sample
+
+
+# ---------------------------------------------------------------- arms ---
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from bsglmm_gb300 import synth
+    study = synth.config1(seed=1)
+    threads = os.cpu_count() or 1
+    rate, sec_per_step, sample = cpu_port_rate(study, threads, args.steps,
+                                               args.warmup, CPU_SAMPLE_VOX)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sec_per_step * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 Wishart)",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "V": study.V, "N": study.N, "P": study.P,
+                   "sample": sample},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def flush_l2(buf):
+    buf.zero_()
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    import bsglmm_gb300 as bsg
+    from bsglmm_gb300 import synth
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    study = synth.config1(seed=1)
+    N, P, S, V = study.N, study.P, study.nsubtypes, study.V
+    s = bsg.Sampler(local)
+    ds = s.add_dataset(study.mask, study.covar, study.data, S)
+    ch = s.add_chain(ds, seed=1 + rank, burnin=0, thin=1)
+    if args.lpv or args.threads:
+        s.set_tuning(args.lpv, args.threads)
+    lpv, thr = s.tuning()
+    flushbuf = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+
+    # warm-up (also instantiates the one-sweep graph)
+    for _ in range(args.warmup):
+        s.run_timed(1)
+    s.sync()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        s.sync()
+
+    barrier()
+    dev_ms = []
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush_l2(flushbuf)
+            torch.cuda.synchronize()
+            dev_ms.append(s.run_timed(1))
+        s.sync()
+        wall = time.perf_counter() - t0
+    barrier()
+    total_ms = float(sum(dev_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * N * V * args.steps / (total_ms * 1e-3)
+
+    # e2e through the C ABI with host buffers (Omega in, Omega + column means out)
+    om = s.omega(ch)
+    h2d = om.nbytes
+    d2h = om.nbytes + 4 * P
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.set_omega(ch, om)
+        s.run(1, sync=False)
+        om = s.omega(ch)
+        _ = s.colmeans(ch)
+    s.sync()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = world * N * V * args.steps / e2e_s
+
+    # live per-kernel timing of the same sweep (CUDA events on the sampler's
+    # stream, plain launches)
+    kms, kl = s.profile(max(args.steps, 5))
+    s.sync()
+    fused_avg_ms = kms[0] / kl[0]
+    flops_launch = N * V / 2 * fused_flops_per_update(P)
+    achieved_tflops = flops_launch / (fused_avg_ms * 1e-3) / 1e12
+    peak = None
+    import ctypes as C
+    pk = C.c_double()
+    if s._L.bsg_fp32_peak(local, C.byref(pk)) == 0:
+        peak = pk.value
+    fused_share = kms[0] / kms[2]
+    launches = s.launches_per_sweep() * args.steps
+
+    if rank != 0:
+        s.close()
+        return
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        crate, _, sample = cpu_port_rate(study, threads, 1, 0, CPU_SAMPLE_VOX)
+        cpu = {"value": crate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": sample}
+    peaks = measured_peaks()
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (f64 Omega/accumulators)", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "V": V, "N": N, "P": P, "S": S,
+                   "chains_per_gpu": 1, "l2": "flushed between timed sweeps",
+                   "lanes_per_voxel": lpv, "block_threads": thr,
+                   "parallelism": f"replicas x{world}"},
+        "sweeps_per_s": 1e3 / ms_per_step,
+        "wall_s": wall,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": {
+            "bound": "fp32", "kernel": "fused_colour_kernel",
+            "achieved": achieved_tflops, "peak": peak, "unit": "TFLOP/s",
+            "frac": (achieved_tflops / peak) if peak else None,
+            "peak_source": "measured FP32 FMA microbenchmark (bsg_fp32_peak)",
+            "traffic": None,
+            "flops_per_update": fused_flops_per_update(P),
+            "fused_avg_launch_ms": fused_avg_ms, "fused_share_of_sweep": fused_share,
+            "hbm_bytes_per_sweep": sweep_bytes(N, V, P, S),
+            "hbm_achieved_gbs": sweep_bytes(N, V, P, S) / (ms_per_step * 1e-3) / 1e9,
+            "hbm_peak_gbs": peaks.get("hbm_gbs"),
+        },
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+    s.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--lpv", type=int, default=0)
+    ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -53,6 +53,7 @@ SIGNATURES = {
     "bsg_get_maps": (_i32, [_P, _i32, _P, _P, _P, _P]),
     "bsg_reset_accumulators": (_i32, [_P, _i32]),
     "bsg_sweep_supplied": (_i32, [_P, _i32, _P, _P, _P, _P, _i32]),
+    "bsg_fp32_peak": (_i32, [_i32, C.POINTER(C.c_double)]),
 }
 
 

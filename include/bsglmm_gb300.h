@@ -154,6 +154,12 @@ bsg_status bsg_sweep_supplied(bsg_ctx *ctx, int32_t chain,
                               const double *chi2, const double *wnorm,
                               int32_t form);
 
+/* ------------------------------------------------------- measurement -- */
+/* FP32 FMA throughput of the device in TFLOP/s (2 flops per FMA), best of
+ * five launches: the denominator of the fused kernel's roofline.  No
+ * counterpart in the reference. */
+bsg_status bsg_fp32_peak(int32_t device, double *tflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -54,6 +54,9 @@ SIGNATURES = {
     "bsg_reset_accumulators": (_i32, [_P, _i32]),
     "bsg_sweep_supplied": (_i32, [_P, _i32, _P, _P, _P, _P, _i32]),
     "bsg_fp32_peak": (_i32, [_i32, C.POINTER(C.c_double)]),
+    "bsg_omega_update_noalloc": (_i32, [_P, _P, _P, _i32, _i32, _i32, _i32, _i32,
+                                        _i32, _P, _P, C.c_uint64, C.c_uint32,
+                                        _i64, _P, _P, _P]),
 }
 
 

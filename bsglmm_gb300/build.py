@@ -29,6 +29,7 @@ SOURCES = [
     "bsg_fused_l8.cu",
     "bsg_kernels.cu",
     "bsg_peak.cu",
+    "bsg_noalloc.cu",
     "bsg_api.cpp",
 ]
 HEADERS = ["bsg_device.cuh", "bsg_fused.cuh", "bsg_internal.h"]

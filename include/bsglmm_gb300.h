@@ -154,6 +154,40 @@ bsg_status bsg_sweep_supplied(bsg_ctx *ctx, int32_t chain,
                               const double *chi2, const double *wnorm,
                               int32_t form);
 
+/* ------------------------------------------------ allocation-free call -- */
+/* Largest V accepted by bsg_omega_update_noalloc. */
+#define BSG_NOALLOC_MAX_VOXELS 4194304
+
+/* The Omega | beta Wishart draw of one chain, for callers that cannot
+ * allocate device memory (a plugin inside a runtime that owns every
+ * allocation, a pipeline that allocates only at start-up): it calls no
+ * cudaMalloc/cudaFree and no allocating library routine.  No counterpart in
+ * the reference (whose updateSpatCoefPrecGPU mallocs per call,
+ * covarGPU.cu:1072).
+ *
+ * All pointers are device memory owned by the caller: spatcoef [P][Vp],
+ * vox [V] padded indices of the in-mask voxels (colour 0 then colour 1 as
+ * bsg_get_lattice returns them), idxsc the padded -> compact dilated map,
+ * omega [P][P] (output, FP64), status (optional, 1 int: 0 or error bits).
+ * chi2 [P] and wnorm [P(P-1)/2] supply the Bartlett variates; pass both
+ * NULL to draw them from (seed, chain_id, sweep) as bsg_run does.
+ *
+ * Its reduction scratch is a fixed 1.4 MB array inside the library, held
+ * by every GPU that loads it until exit and shared by every call on that
+ * device: calls that can overlap on the GPU race and must be serialised by
+ * the caller.  The first call on each device looks the array up
+ * (cudaGetSymbolAddress); make that call before any stream capture.
+ * Asynchronous on `stream`.  V > BSG_NOALLOC_MAX_VOXELS returns
+ * BSG_ERR_UNSUPPORTED. */
+bsg_status bsg_omega_update_noalloc(const float *spatcoef, const int32_t *vox,
+                                    const int32_t *idxsc, int32_t nrow,
+                                    int32_t ncol, int32_t V, int32_t Vp,
+                                    int32_t P, int32_t df_offset,
+                                    const double *chi2, const double *wnorm,
+                                    uint64_t seed, uint32_t chain_id,
+                                    int64_t sweep, double *omega,
+                                    int32_t *status, void *stream);
+
 /* ------------------------------------------------------- measurement -- */
 /* FP32 FMA throughput of the device in TFLOP/s (2 flops per FMA), best of
  * five launches: the denominator of the fused kernel's roofline.  No

@@ -32,7 +32,7 @@ SOURCES = [
     "bsg_noalloc.cu",
     "bsg_api.cpp",
 ]
-HEADERS = ["bsg_device.cuh", "bsg_fused.cuh", "bsg_internal.h"]
+HEADERS = ["bsg_device.cuh", "bsg_fused.cuh", "bsg_internal.h", "bsg_math.cuh"]
 
 
 def nvcc() -> str:

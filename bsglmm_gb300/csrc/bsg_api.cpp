@@ -71,7 +71,7 @@ struct bsg_ctx {
   std::vector<Group> groups;
   BlockMap *d_post_map = nullptr;
   int post_blocks = 0;
-  int lpv = 1, threads = 128;
+  int lpv = 1, threads = 256;
   std::map<int64_t, cudaGraphExec_t> graphs;
   std::string err;
 };
@@ -514,15 +514,15 @@ bsg_status bsg_add_chain(bsg_ctx *ctx, int32_t dataset_id,
   CK(e);
   CK(cudaMemset(cv.colmean, 0, sizeof(float) * P));
   const size_t nacc = (size_t)P * d.V, nprb = (size_t)d.S * d.V;
-  cv.acc_mean = (double *)dalloc(ctx, sizeof(double) * nacc, &e);
+  cv.acc_sum = (double *)dalloc(ctx, sizeof(double) * nacc, &e);
   CK(e);
-  cv.acc_m2 = (double *)dalloc(ctx, sizeof(double) * nacc, &e);
+  cv.acc_sq = (double *)dalloc(ctx, sizeof(double) * nacc, &e);
   CK(e);
-  cv.acc_prb = (double *)dalloc(ctx, sizeof(double) * (nprb ? nprb : 1), &e);
+  cv.prb_sum = (double *)dalloc(ctx, sizeof(double) * (nprb ? nprb : 1), &e);
   CK(e);
-  CK(cudaMemset(cv.acc_mean, 0, sizeof(double) * nacc));
-  CK(cudaMemset(cv.acc_m2, 0, sizeof(double) * nacc));
-  if (nprb) CK(cudaMemset(cv.acc_prb, 0, sizeof(double) * nprb));
+  CK(cudaMemset(cv.acc_sum, 0, sizeof(double) * nacc));
+  CK(cudaMemset(cv.acc_sq, 0, sizeof(double) * nacc));
+  if (nprb) CK(cudaMemset(cv.prb_sum, 0, sizeof(double) * nprb));
   cv.partials = (double *)dalloc(ctx, sizeof(double) * (size_t)cv.post_blocks * kPostVals, &e);
   CK(e);
   ChainCounters *cnt = (ChainCounters *)dalloc(ctx, sizeof(ChainCounters), &e);
@@ -806,15 +806,21 @@ bsg_status bsg_get_posterior(bsg_ctx *ctx, int32_t chain, double *mean,
   bsg_status s = bsg_get_sweep(ctx, chain, nullptr, &nk);
   if (s) return s;
   const size_t n = (size_t)d.P * d.V;
-  if (mean) CK(cudaMemcpy(mean, c.dev.acc_mean, sizeof(double) * n, cudaMemcpyDeviceToHost));
-  if (var) {
-    CK(cudaMemcpy(var, c.dev.acc_m2, sizeof(double) * n, cudaMemcpyDeviceToHost));
-    const double den = (double)(nk - 1);
-    for (size_t i = 0; i < n; ++i) var[i] /= den;
+  // mean = sum / T, var = (sum2 - T mean^2) / (T - 1)  (mcmc.cpp:877-881)
+  std::vector<double> sum(n), sq(n);
+  CK(cudaMemcpy(sum.data(), c.dev.acc_sum, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(sq.data(), c.dev.acc_sq, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  const double T = (double)nk;
+  for (size_t i = 0; i < n; ++i) {
+    const double m = sum[i] / T;
+    if (mean) mean[i] = m;
+    if (var) var[i] = (sq[i] - T * m * m) / (T - 1.0);
   }
-  if (prb && d.S)
-    CK(cudaMemcpy(prb, c.dev.acc_prb, sizeof(double) * (size_t)d.S * d.V,
+  if (prb && d.S) {
+    CK(cudaMemcpy(prb, c.dev.prb_sum, sizeof(double) * (size_t)d.S * d.V,
                   cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < (size_t)d.S * d.V; ++i) prb[i] /= T;
+  }
   if (nkept) *nkept = nk;
   return BSG_OK;
 }
@@ -861,9 +867,9 @@ bsg_status bsg_reset_accumulators(bsg_ctx *ctx, int32_t chain) {
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   const size_t n = (size_t)d.P * d.V;
-  CK(cudaMemset(c.dev.acc_mean, 0, sizeof(double) * n));
-  CK(cudaMemset(c.dev.acc_m2, 0, sizeof(double) * n));
-  if (d.S) CK(cudaMemset(c.dev.acc_prb, 0, sizeof(double) * (size_t)d.S * d.V));
+  CK(cudaMemset(c.dev.acc_sum, 0, sizeof(double) * n));
+  CK(cudaMemset(c.dev.acc_sq, 0, sizeof(double) * n));
+  if (d.S) CK(cudaMemset(c.dev.prb_sum, 0, sizeof(double) * (size_t)d.S * d.V));
   CK(cudaMemset(c.dev.nkept, 0, sizeof(long long)));
   return BSG_OK;
 }

@@ -6,6 +6,7 @@
 #include <cstdint>
 
 #include "bsg_internal.h"
+#include "bsg_math.cuh"
 
 namespace bsg {
 
@@ -15,7 +16,12 @@ namespace bsg {
 // 0x9E3779B9 / 0xBB67AE85.  Stateless: every variate of the sampler is a
 // pure function of (counter, key), so results do not depend on the launch
 // shape and resuming from a checkpoint is exact.
+#ifndef BSG_PHILOX_ROUND_KEYS
+#define BSG_PHILOX_ROUND_KEYS 0  // 1: keep the 10 round keys in registers
+#endif
+
 struct PhiloxKey {
+#if BSG_PHILOX_ROUND_KEYS
   uint32_t k0[10], k1[10];  // round keys, precomputed once per thread
   __device__ __forceinline__ void init(uint32_t a, uint32_t b) {
 #pragma unroll
@@ -24,6 +30,21 @@ struct PhiloxKey {
       k1[r] = b + (uint32_t)r * 0xBB67AE85u;
     }
   }
+  __device__ __forceinline__ uint32_t r0(int r) const { return k0[r]; }
+  __device__ __forceinline__ uint32_t r1(int r) const { return k1[r]; }
+#else
+  uint32_t a0, a1;  // round keys formed on the fly
+  __device__ __forceinline__ void init(uint32_t a, uint32_t b) {
+    a0 = a;
+    a1 = b;
+  }
+  __device__ __forceinline__ uint32_t r0(int r) const {
+    return a0 + (uint32_t)r * 0x9E3779B9u;
+  }
+  __device__ __forceinline__ uint32_t r1(int r) const {
+    return a1 + (uint32_t)r * 0xBB67AE85u;
+  }
+#endif
 };
 
 __device__ __forceinline__ uint4 philox(uint4 c, const PhiloxKey &k) {
@@ -31,7 +52,7 @@ __device__ __forceinline__ uint4 philox(uint4 c, const PhiloxKey &k) {
   for (int r = 0; r < 10; ++r) {
     const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
     const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
-    c = make_uint4(hi1 ^ c.y ^ k.k0[r], lo1, hi0 ^ c.w ^ k.k1[r], lo0);
+    c = make_uint4(hi1 ^ c.y ^ k.r0(r), lo1, hi0 ^ c.w ^ k.r1(r), lo0);
   }
   return c;
 }
@@ -65,7 +86,7 @@ __device__ __forceinline__ double u_of_d(uint32_t k) {
 // Standard normal by inversion with exact tails.
 __device__ __forceinline__ float normal_of(uint32_t k) {
   const bool lo = k < 0x80000000u;
-  const float t = normcdfinvf(u_of(lo ? k : ~k));
+  const float t = ndtri_lower(u_of(lo ? k : ~k));
   return lo ? t : -t;
 }
 
@@ -73,12 +94,12 @@ __device__ __forceinline__ float normal_of(uint32_t k) {
 //   t = Phi^-1(Phi(a) + u Q(a)),  evaluated as -Phi^-1(Q(a) (1-u)) once the
 // argument passes 1/2, so both tails keep relative precision.
 __device__ __forceinline__ float tn_lower_inv(float a, uint32_t k) {
-  const float T = normcdff(-fabsf(a));  // mass beyond |a|
+  const float T = phi_tail(fabsf(a));  // mass beyond |a|
   const float Pa = a < 0.f ? T : 1.f - T;
   const float Qa = a < 0.f ? 1.f - T : T;
   const float pl = fmaf(u_of(k), Qa, Pa);
   const bool lo = pl < 0.5f;
-  const float t = normcdfinvf(lo ? pl : Qa * u_of(~k));
+  const float t = ndtri_lower(lo ? pl : Qa * u_of(~k));
   return lo ? t : -t;
 }
 

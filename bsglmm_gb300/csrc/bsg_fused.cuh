@@ -21,8 +21,20 @@
 
 namespace bsg {
 
+// Resident 256-thread blocks per SM asked of ptxas: three (85 registers) up
+// to P = 5, two (128 registers) above, measured fastest on the brain-sized
+// study; BSG_FUSED_MIN_BLOCKS overrides it for tuning builds.
+template <int P>
+constexpr int fused_min_blocks() {
+#ifdef BSG_FUSED_MIN_BLOCKS
+  return BSG_FUSED_MIN_BLOCKS;
+#else
+  return P <= 5 ? 3 : 2;
+#endif
+}
+
 template <int P, int LPV, bool SUPP>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, fused_min_blocks<P>())
     fused_colour_kernel(const DatasetDev *__restrict__ dsv,
                         ChainDev *__restrict__ chv,
                         const BlockMap *__restrict__ map, int colour,
@@ -78,40 +90,61 @@ __global__ void __launch_bounds__(256)
     }
     __syncthreads();
     if (active) {
+      // One subject: mu = bwm + x'beta; a = -mu if Y = 1 else mu (sign-bit
+      // flip by ymask = Y << 31); t ~ N(0,1) on (a, inf);
+      // Z - bwm = x'beta + (Y ? t : -t); acc += x (Z - bwm).
+      auto subject = [&](int col, uint32_t ymask, uint32_t kk, uint32_t isub) {
+        float x[P];
+        float m0 = 0.f;
+#pragma unroll
+        for (int p = 0; p < P; ++p) {
+          x[p] = Xs[p][col];
+          m0 = fmaf(beta[p], x[p], m0);
+        }
+        const float a = __uint_as_float(__float_as_uint(m0 + bwm) ^ ymask);
+        float t;
+        if (SUPP || a <= kATail) {
+          t = tn_lower_inv(a, kk);
+        } else {
+          t = tn_lower_tail(a, isub, (uint32_t)v, sweep, cid | kTagZTail,
+                            ch.key0, ch.key1, &ok);
+        }
+        const float zr = m0 + __uint_as_float(__float_as_uint(t) ^ ymask ^ 0x80000000u);
+#pragma unroll
+        for (int p = 0; p < P; ++p) acc[p] = fmaf(x[p], zr, acc[p]);
+      };
+      auto variate = [&](uint4 r, int q, uint32_t isub) -> uint32_t {
+        if (SUPP) return __ldg(sup.ubits + (size_t)isub * d.V + v);
+        return pick4(r, q);
+      };
       const int nw = (cn + 31) >> 5;
       for (int wl = k; wl < nw; wl += LPV) {
         const int w = (i0 >> 5) + wl;
-        const uint32_t yw = __ldg(yb + (size_t)w * nc + j);
+        uint32_t yw = __ldg(yb + (size_t)w * nc + j);
         const int nbits = min(32, cn - (wl << 5));
         const int xo = (wl << 5) + wl;  // padded offset of bit 0
-        for (int b = 0; b < nbits; b += 4) {
-          const uint32_t i = (uint32_t)(i0 + (wl << 5) + b);
-          uint4 r = make_uint4(0, 0, 0, 0);
-          if (!SUPP) r = philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key);
+        const uint32_t i00 = (uint32_t)(i0 + (wl << 5));
+        if (nbits == 32) {
+#pragma unroll 1
+          for (int b = 0; b < 32; b += 4) {
+            const uint32_t i = i00 + (uint32_t)b;
+            uint4 r = make_uint4(0, 0, 0, 0);
+            if (!SUPP) r = philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key);
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            if (b + q < nbits) {
-              float x[P];
-              float mu = bwm;
+            for (int q = 0; q < 4; ++q) {
+              subject(xo + b + q, yw << 31, variate(r, q, i + q), i + q);
+              yw >>= 1;
+            }
+          }
+        } else {
+          for (int b = 0; b < nbits; b += 4) {
+            const uint32_t i = i00 + (uint32_t)b;
+            uint4 r = make_uint4(0, 0, 0, 0);
+            if (!SUPP) r = philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key);
 #pragma unroll
-              for (int p = 0; p < P; ++p) {
-                x[p] = Xs[p][xo + b + q];
-                mu = fmaf(beta[p], x[p], mu);
-              }
-              const bool y = (yw >> (b + q)) & 1u;
-              const float a = y ? -mu : mu;
-              float t;
-              if (SUPP) {
-                t = tn_lower_inv(a, __ldg(sup.ubits + (size_t)(i + q) * d.V + v));
-              } else if (a <= kATail) {
-                t = tn_lower_inv(a, pick4(r, q));
-              } else {
-                t = tn_lower_tail(a, i + q, (uint32_t)v, sweep, cid | kTagZTail,
-                                  ch.key0, ch.key1, &ok);
-              }
-              const float zr = (y ? mu + t : mu - t) - bwm;
-#pragma unroll
-              for (int p = 0; p < P; ++p) acc[p] = fmaf(x[p], zr, acc[p]);
+            for (int q = 0; q < 4; ++q) {
+              if (b + q < nbits) subject(xo + b + q, yw << 31, variate(r, q, i + q), i + q);
+              yw >>= 1;
             }
           }
         }

@@ -63,9 +63,9 @@ struct ChainDev {
   float *omega_f;          // [P*P] float copy read by the colour kernels
   double *omega_d;         // [P*P]
   float *colmean;          // [P]
-  double *acc_mean;        // [P][V]
-  double *acc_m2;          // [P][V]
-  double *acc_prb;         // [S][V]
+  double *acc_sum;         // [P][V]  sum of beta over kept sweeps
+  double *acc_sq;          // [P][V]  sum of beta^2
+  double *prb_sum;         // [S][V]  sum of the lesion probability
   double *partials;        // [post_blocks][kPostVals]
   unsigned int *done;      // arrival counter of the post-sweep kernel
   long long *sweep;        // index of the sweep being drawn

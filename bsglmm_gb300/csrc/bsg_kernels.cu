@@ -49,39 +49,6 @@ cudaError_t launch_fused(int P, int lpv, int threads, bool supplied,
 }
 
 // ----------------------------------------------------- FP64 Wishart tail --
-// Dense helpers on element (r, c) at A[c + r*n] (cholesky.cpp layout).
-__device__ static bool chol_full(double *A, int n) {
-  for (int k = 0; k < n; ++k) {
-    double dkk = A[k + k * n];
-    if (!(dkk > 0.0)) return false;
-    dkk = sqrt(dkk);
-    A[k + k * n] = dkk;
-    for (int j = k + 1; j < n; ++j) A[k + j * n] /= dkk;
-    for (int j = k + 1; j < n; ++j)
-      for (int i = j; i < n; ++i) A[j + i * n] -= A[k + i * n] * A[k + j * n];
-  }
-  return true;
-}
-
-// Inverse of G G' from the lower factor (cholesky.cpp:55-86 scheme).
-__device__ static void chol_inverse(const double *G, int n, double *out) {
-  double col[kMaxP];
-  for (int k = 0; k < n; ++k) {
-    for (int i = 0; i < n; ++i) col[i] = (i == k) ? 1.0 : 0.0;
-    for (int i = 0; i < n; ++i) {
-      double s = 0.0;
-      for (int j = 0; j < i; ++j) s += G[j + i * n] * col[j];
-      col[i] = (col[i] - s) / G[i + i * n];
-    }
-    for (int i = n - 1; i >= 0; --i) {
-      double s = 0.0;
-      for (int j = i + 1; j < n; ++j) s += G[i + j * n] * col[j];
-      col[i] = (col[i] - s) / G[i + i * n];
-    }
-    for (int i = 0; i < n; ++i) out[k + i * n] = col[i];
-  }
-}
-
 // Marsaglia & Tsang (2000) gamma(a, 1); a < 1 through the U^(1/a) boost.
 // Attempt t of slot uses counter (slot*64 + t, 0, sweep, chain<<8|GAMMA).
 __device__ static double gamma_mt(double a, uint32_t slot, uint32_t sweep,
@@ -105,92 +72,148 @@ __device__ static double gamma_mt(double a, uint32_t slot, uint32_t sweep,
   return dd;
 }
 
+// In-place Cholesky of the lower triangle of the P x P matrix A (row-major
+// A[r*kMaxP + c]) by one warp, rows across lanes (the outer-product scheme
+// of cholesky.cpp:13-33).  Returns false (warp-uniform) on a non-positive
+// pivot.
+__device__ static bool chol_warp(double (*A)[kMaxP], int P, int lane) {
+  bool ok = true;
+  for (int k = 0; k < P; ++k) {
+    const double d = A[k][k];
+    ok = ok && (d > 0.0);
+    const double s = sqrt(d);
+    __syncwarp();
+    if (lane == k) A[k][k] = s;
+    if (lane > k && lane < P) A[lane][k] /= s;
+    __syncwarp();
+    if (lane > k && lane < P)
+      for (int j = k + 1; j <= lane; ++j) A[lane][j] -= A[lane][k] * A[j][k];
+    __syncwarp();
+  }
+  return ok;
+}
+
 // Omega | beta ~ Wishart(df, (S + I)^-1) by the Bartlett construction of
 // rwishart2 (cholesky.cpp:245-286) after chol -> invert -> chol
-// (covar.cpp:286-291, covarGPU.cu:1099-1104), all in FP64.
-__device__ static void wishart_tail(ChainDev &ch, const DatasetDev &d,
+// (covar.cpp:286-291, covarGPU.cu:1099-1104), FP64, one warp.
+__device__ static void wishart_warp(ChainDev &ch, const DatasetDev &d,
                                     const double *tot, long long sweep,
                                     bool kept, long long nk, int supplied,
-                                    const Supplied &sup) {
+                                    const Supplied &sup, int lane) {
+  __shared__ double A[kMaxP][kMaxP], Ai[kMaxP][kMaxP], T[kMaxP][kMaxP],
+      B[kMaxP][kMaxP];
   const int P = d.P;
-  double A[kMaxP * kMaxP], Ai[kMaxP * kMaxP], T[kMaxP * kMaxP];
-  double B[kMaxP * kMaxP];
   int err = 0;
-  for (int r = 0; r < P; ++r)
-    for (int c = 0; c <= r; ++c)
-      A[c + r * P] = A[r + c * P] = tot[tri(r, c)] + (r == c ? 1.0 : 0.0);
-  bool ok = chol_full(A, P);
+  if (lane < P)
+    for (int c = 0; c < P; ++c) {
+      const int r = lane;
+      A[r][c] = (r >= c ? tot[tri(r, c)] : tot[tri(c, r)]) + (r == c ? 1.0 : 0.0);
+      T[r][c] = 0.0;
+    }
+  __syncwarp();
+  bool ok = chol_warp(A, P, lane);
   if (ok) {
-    chol_inverse(A, P, Ai);
-    ok = chol_full(Ai, P);
+    // column `lane` of (G G')^-1 by forward then back substitution
+    if (lane < P) {
+      double col[kMaxP];
+      for (int i = 0; i < P; ++i) col[i] = (i == lane) ? 1.0 : 0.0;
+      for (int i = 0; i < P; ++i) {
+        double s = 0.0;
+        for (int j = 0; j < i; ++j) s += A[i][j] * col[j];
+        col[i] = (col[i] - s) / A[i][i];
+      }
+      for (int i = P - 1; i >= 0; --i) {
+        double s = 0.0;
+        for (int j = i + 1; j < P; ++j) s += A[j][i] * col[j];
+        col[i] = (col[i] - s) / A[i][i];
+      }
+      for (int i = 0; i < P; ++i) Ai[lane][i] = col[i];  // row `lane` of Ai
+    }
+    __syncwarp();
+    ok = chol_warp(Ai, P, lane);
   }
   if (ok) {
     const double df = (double)d.V + (double)ch.df_offset;
     const uint32_t cid = ch.chain_id << 8, sw = (uint32_t)sweep;
-    for (int i = 0; i < P * P; ++i) T[i] = 0.0;
-    for (int i = 0; i < P; ++i) {
-      const double c2 = supplied ? sup.chi2[i]
-                                 : 2.0 * gamma_mt(0.5 * (df - i), (uint32_t)i,
+    if (lane < P) {
+      const double c2 = supplied ? sup.chi2[lane]
+                                 : 2.0 * gamma_mt(0.5 * (df - lane), (uint32_t)lane,
                                                   sw, cid | kTagGamma, ch.key0,
                                                   ch.key1, &err);
-      T[i + i * P] = sqrt(c2);
-      for (int j = 0; j < i; ++j) {
-        const int m = i * (i - 1) / 2 + j;
-        double z;
-        if (supplied) {
-          z = sup.wnorm[m];
-        } else {
-          const uint4 r = philox1(make_uint4((uint32_t)(m >> 2), 0u, sw,
-                                             cid | kTagWNorm),
-                                  ch.key0, ch.key1);
-          z = (double)normal_of(pick4(r, m & 3));
-        }
-        T[j + i * P] = z;
+      T[lane][lane] = sqrt(c2);
+    }
+    const int nw = P * (P - 1) / 2;
+    if (lane < nw) {
+      int i = 1;
+      while ((i + 1) * i / 2 <= lane) ++i;  // row i: lane in [i(i-1)/2, i(i+1)/2)
+      const int j = lane - i * (i - 1) / 2;
+      double z;
+      if (supplied) {
+        z = sup.wnorm[lane];
+      } else {
+        const uint4 r = philox1(make_uint4((uint32_t)(lane >> 2), 0u, sw,
+                                           cid | kTagWNorm),
+                                ch.key0, ch.key1);
+        z = (double)normal_of(pick4(r, lane & 3));
+      }
+      T[i][j] = z;
+    }
+    __syncwarp();
+    if (lane < P) {  // row `lane` of B = L T (L lower from Ai)
+      const int i = lane;
+      for (int j = 0; j < P; ++j) {
+        double s = 0.0;
+        for (int k = j; k <= i; ++k) s += Ai[i][k] * T[k][j];
+        B[i][j] = j <= i ? s : 0.0;
       }
     }
-    for (int i = 0; i < P; ++i)
-      for (int j = 0; j <= i; ++j) {
-        double s = 0.0;
-        for (int k = j; k <= i; ++k) s += Ai[k + i * P] * T[j + k * P];
-        B[j + i * P] = s;
-      }
+    __syncwarp();
     bool fin = true;
-    for (int i = 0; i < P; ++i)
+    if (lane < P) {
+      const int i = lane;
       for (int j = 0; j < P; ++j) {
         const int K = i < j ? i : j;
         double s = 0.0;
-        for (int k = 0; k <= K; ++k) s += B[k + i * P] * B[k + j * P];
-        A[j + i * P] = s;
+        for (int k = 0; k <= K; ++k) s += B[i][k] * B[j][k];
+        A[i][j] = s;  // A is free again
         fin = fin && isfinite(s);
       }
+    }
+    fin = __all_sync(0xffffffffu, fin);
+    __syncwarp();
     if (fin) {
-      for (int i = 0; i < P * P; ++i) {
-        ch.omega_d[i] = A[i];
-        ch.omega_f[i] = (float)A[i];
-      }
+      if (lane < P)
+        for (int j = 0; j < P; ++j) {
+          ch.omega_d[lane * P + j] = A[lane][j];
+          ch.omega_f[lane * P + j] = (float)A[lane][j];
+        }
     } else {
       err |= kErrNaN;
     }
   } else {
     err |= kErrWishart;
   }
-  for (int p = 0; p < P; ++p)
-    ch.colmean[p] = (float)(tot[kMaxPairs + p] / (double)d.V);
-  if (err) atomicOr(ch.status, err);
-  *ch.sweep = sweep + 1;
-  if (kept) *ch.nkept = nk + 1;
-  *ch.done = 0u;
-  __threadfence();
+  if (lane < P) ch.colmean[lane] = (float)(tot[kMaxPairs + lane] / (double)d.V);
+  err = __reduce_or_sync(0xffffffffu, err);
+  if (lane == 0) {
+    if (err) atomicOr(ch.status, err);
+    *ch.sweep = sweep + 1;
+    if (kept) *ch.nkept = nk + 1;
+    *ch.done = 0u;
+    __threadfence();
+  }
 }
 
 // ------------------------------------------------------ post-sweep pass --
 // One pass over every in-mask voxel after both colours: the pair sums of
 // Spat_Coef_Prec (covarGPU.cu:953-1013, covar.cpp:220-262; the indicator
 // tests the row coefficient of the forward neighbour), the column sums of
-// covarGPU.cu:563-583, and on kept sweeps the FP64 Welford accumulators of
-// beta and of the lesion probability (mcmc.cpp:627-649).  Block partials
-// are summed in block order by the last block to arrive, which then draws
-// Omega: the result is bitwise reproducible.
+// covarGPU.cu:563-583, and on kept sweeps the FP64 running sums of beta,
+// beta^2 and the lesion probability (mcmc.cpp:627-649).  Each thread sums
+// the products of its (at most four) voxels in FP32 and adds them to FP64
+// accumulators; block partials are summed in a fixed order by the last
+// block to arrive, whose first warp then draws Omega: the result is
+// bitwise reproducible.
 __global__ void __launch_bounds__(kPostThreads)
     post_sweep_kernel(const DatasetDev *__restrict__ dsv,
                       ChainDev *__restrict__ chv,
@@ -208,14 +231,13 @@ __global__ void __launch_bounds__(kPostThreads)
   const long long sweep = *ch.sweep, nk = *ch.nkept;
   const int thin = ch.thin > 0 ? ch.thin : 1;
   const bool kept = sweep > ch.burnin && (sweep % thin) == 0;
-  const double inv_n = 1.0 / (double)(nk + 1);
   const int npairs = P * (P + 1) / 2;
 
-  double accp[kMaxPairs], cs[kMaxP];
+  float pv[kMaxPairs], csf[kMaxP];
 #pragma unroll
-  for (int q = 0; q < kMaxPairs; ++q) accp[q] = 0.0;
+  for (int q = 0; q < kMaxPairs; ++q) pv[q] = 0.f;
 #pragma unroll
-  for (int p = 0; p < kMaxP; ++p) cs[p] = 0.0;
+  for (int p = 0; p < kMaxP; ++p) csf[p] = 0.f;
 
   for (int t = 0; t < kPostPerThread; ++t) {
     const int pos = bm.start + threadIdx.x + t * kPostThreads;
@@ -229,11 +251,8 @@ __global__ void __launch_bounds__(kPostThreads)
 #pragma unroll
     for (int p = 0; p < kMaxP; ++p) {
       bs[p] = p < P ? ch.beta[(size_t)p * Vp + sc] : 0.f;
-      cs[p] += (double)bs[p];
+      csf[p] += bs[p];
     }
-    float pv[kMaxPairs];
-#pragma unroll
-    for (int q = 0; q < kMaxPairs; ++q) pv[q] = 0.f;
 #pragma unroll
     for (int f = 0; f < 3; ++f) {  // forward neighbours +x, +y, +z
       const int sn = nbp[(size_t)(2 + 2 * f) * nc + j];
@@ -252,31 +271,19 @@ __global__ void __launch_bounds__(kPostThreads)
           for (int c2 = 0; c2 <= r; ++c2) pv[tri(r, c2)] += dd[r] * dd[c2];
         }
     }
-#pragma unroll
-    for (int q = 0; q < kMaxPairs; ++q)
-      if (q < npairs) accp[q] += (double)pv[q];
-
-    if (kept) {
+    if (kept) {  // running sums of mcmc.cpp:637-645, FP64
       const int v = d.vidx[c][j];
 #pragma unroll
       for (int p = 0; p < kMaxP; ++p)
         if (p < P) {
           const double x = (double)bs[p];
-          double *mp = ch.acc_mean + (size_t)p * V + v;
-          double mn = *mp;
-          const double dl = x - mn;
-          mn += dl * inv_n;
-          *mp = mn;
-          ch.acc_m2[(size_t)p * V + v] += dl * (x - mn);
+          ch.acc_sum[(size_t)p * V + v] += x;
+          ch.acc_sq[(size_t)p * V + v] += x * x;
         }
       const float bwm = ch.beta_wm * (d.wm ? d.wm[v] : 1.f);
 #pragma unroll
       for (int g = 0; g < kMaxP; ++g)
-        if (g < S) {
-          const double pr = (double)prob_sdnorm(bs[g] + bwm);
-          double *pp = ch.acc_prb + (size_t)g * V + v;
-          *pp += (pr - *pp) * inv_n;
-        }
+        if (g < S) ch.prb_sum[(size_t)g * V + v] += (double)prob_sdnorm(bs[g] + bwm);
     }
   }
 
@@ -285,7 +292,7 @@ __global__ void __launch_bounds__(kPostThreads)
   for (int q = 0; q < kPostVals; ++q) {
     const bool live = q < kMaxPairs ? q < npairs : (q - kMaxPairs) < P;
     if (!live) continue;
-    double val = q < kMaxPairs ? accp[q] : cs[q - kMaxPairs];
+    double val = q < kMaxPairs ? (double)pv[q] : (double)csf[q - kMaxPairs];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
     if (lane == 0) red[warp][q] = val;
@@ -309,14 +316,20 @@ __global__ void __launch_bounds__(kPostThreads)
   __syncthreads();
   if (!is_last) return;
   __threadfence();
-  if (threadIdx.x < kPostVals) {
+  // Warp w sums values q = w, w + 8, ...: lanes stride over the blocks,
+  // then a fixed shuffle tree -- same order on every run.
+  for (int q = warp; q < kPostVals; q += kPostThreads / 32) {
+    const bool live = q < kMaxPairs ? q < npairs : (q - kMaxPairs) < P;
     double s = 0.0;
-    for (int b = 0; b < ch.post_blocks; ++b)
-      s += __ldcg(ch.partials + (size_t)b * kPostVals + threadIdx.x);
-    tot[threadIdx.x] = s;
+    if (live)
+      for (int b = lane; b < ch.post_blocks; b += 32)
+        s += __ldcg(ch.partials + (size_t)b * kPostVals + q);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) tot[q] = s;
   }
   __syncthreads();
-  if (threadIdx.x == 0) wishart_tail(ch, d, tot, sweep, kept, nk, supplied, sup);
+  if (warp == 0) wishart_warp(ch, d, tot, sweep, kept, nk, supplied, sup, lane);
 }
 
 cudaError_t launch_post(const DatasetDev *ds, ChainDev *ch,

@@ -591,7 +591,7 @@ static int chain_wishart(const orc_problem *pb, const orc_chain_cfg *cfg,
 
 int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
                   int64_t nsweeps, double *spatcoef, double *omega,
-                  double *acc_mean, double *acc_m2, double *acc_prb,
+                  double *acc_sum, double *acc_sq, double *prb_sum,
                   int64_t *nkept) {
   int N = pb->N, P = pb->P, V = pb->V, Vp = pb->Vp, S = pb->S, err = 0;
   uint32_t k0 = cfg->key0, k1 = cfg->key1, ch = cfg->chain;
@@ -637,24 +637,18 @@ int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
       }
     err |= chain_wishart(pb, cfg, sw, spatcoef, omega);
     int kept = (s > cfg->burnin) && (s % (cfg->thin > 0 ? cfg->thin : 1) == 0);
-    if (kept && acc_mean) {
+    if (kept && acc_sum) { /* running sums of mcmc.cpp:637-645 */
       orc_compute_prb(pb, cfg->beta_wm, spatcoef, prb);
-      int64_t n = ++(*nkept);
-      double inv = 1.0 / (double)n;
+      ++(*nkept);
       for (int p = 0; p < pb->nsize; ++p) {
         if (!pb->msk[p]) continue;
         int v = pb->idx[p], sc = pb->idxsc[p];
         for (int q = 0; q < P; ++q) {
           double x = spatcoef[(size_t)q * Vp + sc];
-          double *mn = acc_mean + (size_t)q * V + v;
-          double d = x - *mn;
-          *mn += d * inv;
-          acc_m2[(size_t)q * V + v] += d * (x - *mn);
+          acc_sum[(size_t)q * V + v] += x;
+          acc_sq[(size_t)q * V + v] += x * x;
         }
-        for (int g = 0; g < S; ++g) {
-          double *mp = acc_prb + (size_t)g * V + v;
-          *mp += (prb[(size_t)g * V + v] - *mp) * inv;
-        }
+        for (int g = 0; g < S; ++g) prb_sum[(size_t)g * V + v] += prb[(size_t)g * V + v];
       }
     }
   }

@@ -103,12 +103,13 @@ typedef struct {
 } orc_chain_cfg;
 
 /* Runs sweeps [s0, s0 + nsweeps) from state (spatcoef, omega) in FP64 using
- * the same counter layout as the GPU sampler.  Accumulates (if acc != NULL)
- * acc_mean[P][V], acc_m2[P][V], acc_prb[S][V] (Welford) and *nkept.
+ * the same counter layout as the GPU sampler.  Accumulates (if acc_sum !=
+ * NULL) the running sums acc_sum[P][V], acc_sq[P][V], prb_sum[S][V] of
+ * mcmc.cpp:637-645 and *nkept.
  * Returns an OR of error flags (0 = ok). */
 int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
                   int64_t nsweeps, double *spatcoef, double *omega,
-                  double *acc_mean, double *acc_m2, double *acc_prb,
+                  double *acc_sum, double *acc_sq, double *prb_sum,
                   int64_t *nkept);
 
 /* ------------------------------- CPU timing port of the reference sweep -- */

@@ -206,14 +206,18 @@ class Problem:
         b = (np.zeros((self.P, self.Vp)) if spatcoef is None
              else np.array(spatcoef, dtype=np.float64, order="C"))
         om = np.eye(self.P) if omega is None else np.array(omega, dtype=np.float64, order="C")
-        mean = np.zeros((self.P, self.V))
-        m2 = np.zeros((self.P, self.V))
-        prb = np.zeros((max(self.S, 1), self.V))
+        s1 = np.zeros((self.P, self.V))
+        s2 = np.zeros((self.P, self.V))
+        sp = np.zeros((max(self.S, 1), self.V))
         nk = C.c_int64(0)
         err = self._L.orc_chain_run(self.h, C.byref(cfg), s0, nsweeps, _p(b), _p(om),
-                                    _p(mean), _p(m2), _p(prb), C.byref(nk))
-        return dict(beta=b, omega=om, mean=mean, m2=m2, prb=prb[: self.S],
-                    nkept=nk.value, err=err)
+                                    _p(s1), _p(s2), _p(sp), C.byref(nk))
+        T = nk.value
+        with np.errstate(invalid="ignore", divide="ignore"):
+            mean = s1 / T
+            var = (s2 - T * mean * mean) / (T - 1)
+        return dict(beta=b, omega=om, mean=mean, var=var, prb=sp[: self.S] / T,
+                    sum=s1, sumsq=s2, nkept=T, err=err)
 
 
 class Port:

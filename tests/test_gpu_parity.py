@@ -149,7 +149,7 @@ def test_accumulators_match_oracle(bsg, oracle_mod):
         o = pb.chain(seed, 9, burnin=2, thin=2)
         assert nk == o["nkept"] == 3  # sweeps 4, 6, 8
         assert np.allclose(mean, o["mean"], rtol=1e-4, atol=1e-4)
-        assert np.allclose(var, o["m2"] / (nk - 1), rtol=1e-3, atol=1e-4)
+        assert np.allclose(var, o["var"], rtol=1e-3, atol=1e-4)
         assert np.allclose(prb, o["prb"], atol=1e-4)
         maps = s.maps(ch)
         m = st.mask.astype(bool)

@@ -1,0 +1,82 @@
+"""CPU check of the FP32 normal-tail and inverse-normal approximations used
+by the latent draws (bsglmm_gb300/csrc/bsg_math.cuh): the coefficients are
+read from the header and both functions are evaluated in float32."""
+from __future__ import annotations
+
+import re
+from pathlib import Path
+
+import numpy as np
+from scipy import special
+
+HDR = Path(__file__).resolve().parents[1] / "bsglmm_gb300" / "csrc" / "bsg_math.cuh"
+
+
+def coeffs():
+    text = HDR.read_text()
+    block = text[text.index("BEGIN-COEFFICIENTS"):text.index("END-COEFFICIENTS")]
+    return {k: np.float32(float(v)) for k, v in
+            re.findall(r"(k\w+)\s*=\s*([-+0-9.eE]+)f", block)}
+
+
+C = coeffs()
+f32 = np.float32
+
+
+def fma(a, b, c):
+    return (a.astype(np.float64) * b + c).astype(np.float32)
+
+
+def phi_tail32(x):
+    x = x.astype(np.float32)
+    hi = (x * x).astype(np.float32)
+    lo = (x.astype(np.float64) ** 2 - hi).astype(np.float32)
+    e = (np.exp(-0.5 * hi.astype(np.float64)).astype(np.float32) *
+         fma(f32(-0.5), lo, f32(1)))
+    n = fma(fma(fma(fma(C["kMillsN4"], x, C["kMillsN3"]), x, C["kMillsN2"]), x,
+                C["kMillsN1"]), x, C["kMillsN0"])
+    d = fma(fma(fma(fma(fma(C["kMillsD5"], x, C["kMillsD4"]), x, C["kMillsD3"]), x,
+                    C["kMillsD2"]), x, C["kMillsD1"]), x, f32(1))
+    return (e * (n / d)).astype(np.float32)
+
+
+def ndtri_lower32(p):
+    p = np.maximum(p.astype(np.float32), f32(1.17549435e-38))
+    q = (p - f32(0.5)).astype(np.float32)
+    r = fma(-q, q, f32(0.180625))
+    xc = q * (fma(fma(fma(C["kPpA3"], r, C["kPpA2"]), r, C["kPpA1"]), r, C["kPpA0"]) /
+              fma(fma(fma(C["kPpB3"], r, C["kPpB2"]), r, C["kPpB1"]), r, f32(1)))
+    s = np.sqrt(-np.log(p.astype(np.float64))).astype(np.float32)
+    t1 = (s - f32(1.6)).astype(np.float32)
+    x1 = -(fma(fma(fma(C["kPpC3"], t1, C["kPpC2"]), t1, C["kPpC1"]), t1, C["kPpC0"]) /
+           fma(fma(C["kPpD2"], t1, C["kPpD1"]), t1, f32(1)))
+    t2 = (s - f32(5)).astype(np.float32)
+    x2 = -(fma(fma(fma(C["kPpE3"], t2, C["kPpE2"]), t2, C["kPpE1"]), t2, C["kPpE0"]) /
+           fma(fma(C["kPpF2"], t2, C["kPpF1"]), t2, f32(1)))
+    xt = np.where(s <= 5, x1, x2)
+    return np.where(q >= f32(-0.425), xc, xt).astype(np.float32)
+
+
+def test_all_coefficients_parsed():
+    assert len(C) == 10 + 19
+
+
+def test_phi_tail_relative_error():
+    x = np.linspace(0, 9, 40001).astype(np.float32)
+    err = np.abs(phi_tail32(x) / special.ndtr(-x.astype(np.float64)) - 1)
+    assert err.max() < 5e-7
+
+
+def test_phi_tail_beyond_fit_range_decays():
+    x = np.array([9.5, 12.0, 20.0, 40.0], np.float32)
+    t = phi_tail32(x)
+    assert np.all(np.isfinite(t)) and np.all(np.diff(t) <= 0)
+    assert np.allclose(t[:2], special.ndtr(-x[:2]), rtol=1e-5)
+
+
+def test_ndtri_lower_relative_error():
+    p = np.concatenate([np.logspace(-37, -1.2, 4000),
+                        np.linspace(0.06, 0.5, 4000)]).astype(np.float32)
+    ref = special.ndtri(p.astype(np.float64))
+    got = ndtri_lower32(p)
+    assert np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1e-2)) < 3e-7

@@ -85,7 +85,7 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
@@ -265,9 +265,9 @@ def run_ours(args, rank, world, local):
 
     # live per-kernel timing of the same sweep (CUDA events on the sampler's
     # stream, plain launches)
-    kms, kl = s.profile(max(args.steps, 5))
+    kms, kl = s.profile(min(max(args.steps, 5), 50))
     s.sync()
-    fused_avg_ms = kms[0] / kl[0]
+    fused_avg_ms = (kms[0] + kms[1]) / (kl[0] + kl[1])
     flops_launch = N * V / 2 * fused_flops_per_update(P)
     achieved_tflops = flops_launch / (fused_avg_ms * 1e-3) / 1e12
     peak = None
@@ -275,7 +275,7 @@ def run_ours(args, rank, world, local):
     pk = C.c_double()
     if s._L.bsg_fp32_peak(local, C.byref(pk)) == 0:
         peak = pk.value
-    fused_share = kms[0] / kms[2]
+    fused_share = (kms[0] + kms[1]) / kms[2]
     launches = s.launches_per_sweep() * args.steps
 
     if rank != 0:
@@ -325,7 +325,7 @@ def run_ours(args, rank, world, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--lpv", type=int, default=0)

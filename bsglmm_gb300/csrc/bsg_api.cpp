@@ -37,6 +37,7 @@ struct Chain {
   int dataset = 0;
   bsg_chain_desc desc{};
   ChainDev dev{};
+  size_t cap0 = 0, cap1 = 0;  // partial rows allocated per colour
 };
 
 struct Group {
@@ -47,9 +48,9 @@ struct Group {
 
 // Small per-chain counters kept together on the device.
 struct ChainCounters {
-  long long sweep;
+  long long sweep[2];  // sweeps completed by the colour-0 / colour-1 kernel
   long long nkept;
-  unsigned int done;
+  unsigned int done[2];
   int status;
 };
 
@@ -69,9 +70,13 @@ struct bsg_ctx {
   size_t d_ds_cap = 0, d_ch_cap = 0;
   bool plan_valid = false;
   std::vector<Group> groups;
-  BlockMap *d_post_map = nullptr;
-  int post_blocks = 0;
   int lpv = 1, threads = 256;
+#ifdef BSG_NO_PDL
+  bool pdl = false;
+#else
+  bool pdl = true;  // overlap each colour kernel's latent phase with the
+                    // previous kernel's tail (programmatic dependent launch)
+#endif
   std::map<int64_t, cudaGraphExec_t> graphs;
   std::string err;
 };
@@ -193,6 +198,40 @@ std::string status_text(int bits) {
   return s;
 }
 
+constexpr int kParityThreads = 128;  // tile of the supplied-variate sweep
+
+// Partial rows of the colour kernels, one per block of a chain: column sums
+// (colour 0) and pairs + column sums (colour 1), sized for the smallest
+// tile the context launches.
+bsg_status ensure_partials(bsg_ctx *ctx, int vpb) {
+  cudaError_t e;
+  for (auto &c : ctx->ch) {
+    const Dataset &d = ctx->ds[c.dataset];
+    const size_t n0 = std::max<size_t>(1, (d.vox[0].size() + vpb - 1) / vpb);
+    const size_t n1 = std::max<size_t>(1, (d.vox[1].size() + vpb - 1) / vpb);
+    if (n0 > c.cap0) {
+      dfree(ctx, c.dev.partials0);
+      c.dev.partials0 = (double *)dalloc(ctx, sizeof(double) * n0 * kMaxP, &e);
+      CK(e);
+      c.cap0 = n0;
+    }
+    if (n1 > c.cap1) {
+      dfree(ctx, c.dev.partials1);
+      c.dev.partials1 = (double *)dalloc(ctx, sizeof(double) * n1 * kPostVals, &e);
+      CK(e);
+      c.cap1 = n1;
+    }
+  }
+  return BSG_OK;
+}
+
+// Block map of one colour for one chain: tiles of vpb voxels; colour 1
+// always has at least one block, whose last arrival draws Omega.
+void map_chain(std::vector<BlockMap> &m, int chain, int n, int vpb, int colour) {
+  if (n == 0 && colour == 1) m.push_back({(int32_t)chain, 0});
+  for (int s = 0; s < n; s += vpb) m.push_back({(int32_t)chain, (int32_t)s});
+}
+
 // Rebuilds the device descriptor arrays and block maps.
 bsg_status build_plan(bsg_ctx *ctx) {
   if (ctx->plan_valid) return BSG_OK;
@@ -211,6 +250,9 @@ bsg_status build_plan(bsg_ctx *ctx) {
     ctx->d_ch = (ChainDev *)dalloc(ctx, sizeof(ChainDev) * ctx->d_ch_cap, &e);
     CK(e);
   }
+  const int vpb = ctx->threads / ctx->lpv;
+  bsg_status ps = ensure_partials(ctx, std::min(vpb, kParityThreads));
+  if (ps) return ps;
   std::vector<DatasetDev> hds;
   for (auto &d : ctx->ds) hds.push_back(d.dev);
   std::vector<ChainDev> hch;
@@ -222,7 +264,6 @@ bsg_status build_plan(bsg_ctx *ctx) {
   for (auto &g : ctx->groups)
     for (int c = 0; c < 2; ++c) dfree(ctx, g.d_map[c]);
   ctx->groups.clear();
-  const int vpb = ctx->threads / ctx->lpv;
   for (size_t ci = 0; ci < ctx->ch.size(); ++ci) {
     const Dataset &d = ctx->ds[ctx->ch[ci].dataset];
     Group *g = nullptr;
@@ -233,25 +274,13 @@ bsg_status build_plan(bsg_ctx *ctx) {
       g = &ctx->groups.back();
       g->P = d.P;
     }
-    for (int c = 0; c < 2; ++c)
-      for (int s = 0; s < (int)d.vox[c].size(); s += vpb)
-        g->map[c].push_back({(int32_t)ci, (int32_t)s});
+    for (int c = 0; c < 2; ++c) map_chain(g->map[c], (int)ci, (int)d.vox[c].size(), vpb, c);
   }
   for (auto &g : ctx->groups)
     for (int c = 0; c < 2; ++c) {
       g.d_map[c] = upload(ctx, g.map[c].data(), g.map[c].size(), &e);
       CK(e);
     }
-  std::vector<BlockMap> pm;
-  for (size_t ci = 0; ci < ctx->ch.size(); ++ci) {
-    const Dataset &d = ctx->ds[ctx->ch[ci].dataset];
-    const int ntot = d.V, per = kPostThreads * kPostPerThread;
-    for (int s = 0; s < ntot; s += per) pm.push_back({(int32_t)ci, (int32_t)s});
-  }
-  dfree(ctx, ctx->d_post_map);
-  ctx->d_post_map = upload(ctx, pm.data(), pm.size(), &e);
-  CK(e);
-  ctx->post_blocks = (int)pm.size();
   while (ctx->side.size() < ctx->groups.size()) {
     cudaStream_t s;
     cudaEvent_t ev;
@@ -265,8 +294,8 @@ bsg_status build_plan(bsg_ctx *ctx) {
 }
 
 // Enqueues one sweep of every chain: per P group the two colour kernels
-// (groups on parallel branches when there are several), then the
-// post-sweep pass.
+// (groups on parallel branches when there are several); the colour-1
+// kernel also reduces the Omega pairs and draws Omega.
 cudaError_t enqueue_sweep(bsg_ctx *ctx, cudaStream_t st) {
   const Supplied sup{};
   cudaError_t e;
@@ -274,7 +303,8 @@ cudaError_t enqueue_sweep(bsg_ctx *ctx, cudaStream_t st) {
     const Group &g = ctx->groups[0];
     for (int c = 0; c < 2; ++c) {
       e = launch_fused(g.P, ctx->lpv, ctx->threads, false, ctx->d_ds,
-                       ctx->d_ch, g.d_map[c], (int)g.map[c].size(), c, sup, st);
+                       ctx->d_ch, g.d_map[c], (int)g.map[c].size(), c, sup, st,
+                       ctx->pdl);
       if (e != cudaSuccess) return e;
     }
   } else {
@@ -285,15 +315,15 @@ cudaError_t enqueue_sweep(bsg_ctx *ctx, cudaStream_t st) {
       if ((e = cudaStreamWaitEvent(s, ctx->fork, 0)) != cudaSuccess) return e;
       for (int c = 0; c < 2; ++c) {
         e = launch_fused(g.P, ctx->lpv, ctx->threads, false, ctx->d_ds,
-                         ctx->d_ch, g.d_map[c], (int)g.map[c].size(), c, sup, s);
+                         ctx->d_ch, g.d_map[c], (int)g.map[c].size(), c, sup, s,
+                         ctx->pdl);
         if (e != cudaSuccess) return e;
       }
       if ((e = cudaEventRecord(ctx->join[gi], s)) != cudaSuccess) return e;
       if ((e = cudaStreamWaitEvent(st, ctx->join[gi], 0)) != cudaSuccess) return e;
     }
   }
-  return launch_post(ctx->d_ds, ctx->d_ch, ctx->d_post_map, ctx->post_blocks,
-                     false, sup, st);
+  return cudaSuccess;
 }
 
 bsg_status get_graph(bsg_ctx *ctx, int64_t nsw, cudaGraphExec_t *out) {
@@ -328,7 +358,7 @@ bool valid_chain(const bsg_ctx *ctx, int32_t c) {
 
 
 ChainCounters *counters_of(const Chain &c) {
-  return reinterpret_cast<ChainCounters *>(c.dev.sweep);
+  return reinterpret_cast<ChainCounters *>(c.dev.sweep);  // first member
 }
 
 }  // namespace
@@ -451,7 +481,14 @@ bsg_status bsg_add_dataset(bsg_ctx *ctx, const bsg_dataset_desc *desc,
     }
     dv.nb[c] = upload(ctx, nb.data(), nb.size(), &e);
     CK(e);
-    dv.nnb[c] = upload(ctx, d.nbrs[c].data(), d.nbrs[c].size(), &e);
+    std::vector<uint8_t> nbm(nc);
+    for (int j = 0; j < nc; ++j) {
+      const int p = d.vox[c][j];
+      unsigned m = 0;
+      for (int t = 0; t < 6; ++t) m |= (d.idx[p + off[t]] >= 0 ? 1u : 0u) << t;
+      nbm[j] = (uint8_t)m;
+    }
+    dv.nbm[c] = upload(ctx, nbm.data(), nbm.size(), &e);
     CK(e);
     dv.vidx[c] = upload(ctx, vi.data(), vi.size(), &e);
     CK(e);
@@ -497,8 +534,6 @@ bsg_status bsg_add_chain(bsg_ctx *ctx, int32_t dataset_id,
   cv.df_offset = desc->df_offset;
   cv.burnin = desc->burnin;
   cv.thin = desc->thin;
-  const int per = kPostThreads * kPostPerThread;
-  cv.post_blocks = (d.V + per - 1) / per;
   const int P = d.P;
   cv.beta = (float *)dalloc(ctx, sizeof(float) * (size_t)P * d.Vp, &e);
   CK(e);
@@ -523,14 +558,12 @@ bsg_status bsg_add_chain(bsg_ctx *ctx, int32_t dataset_id,
   CK(cudaMemset(cv.acc_sum, 0, sizeof(double) * nacc));
   CK(cudaMemset(cv.acc_sq, 0, sizeof(double) * nacc));
   if (nprb) CK(cudaMemset(cv.prb_sum, 0, sizeof(double) * nprb));
-  cv.partials = (double *)dalloc(ctx, sizeof(double) * (size_t)cv.post_blocks * kPostVals, &e);
-  CK(e);
   ChainCounters *cnt = (ChainCounters *)dalloc(ctx, sizeof(ChainCounters), &e);
   CK(e);
   CK(cudaMemset(cnt, 0, sizeof(ChainCounters)));
-  cv.sweep = &cnt->sweep;
+  cv.sweep = cnt->sweep;
   cv.nkept = &cnt->nkept;
-  cv.done = &cnt->done;
+  cv.done = cnt->done;
   cv.status = &cnt->status;
   ctx->ch.push_back(c);
   *chain_id = (int32_t)ctx->ch.size() - 1;
@@ -635,17 +668,14 @@ bsg_status bsg_profile(bsg_ctx *ctx, int64_t nsweeps, double *ms,
   const Supplied sup{};
   int64_t nl[3] = {0, 0, 0};
   for (int64_t i = 0; i < nsweeps; ++i) {
-    CK(cudaEventRecord(ev[3 * i], ctx->stream));
-    for (const Group &g : ctx->groups)
-      for (int c = 0; c < 2; ++c) {
+    for (int c = 0; c < 2; ++c) {
+      CK(cudaEventRecord(ev[3 * i + c], ctx->stream));
+      for (const Group &g : ctx->groups) {
         CK(launch_fused(g.P, ctx->lpv, ctx->threads, false, ctx->d_ds, ctx->d_ch,
                         g.d_map[c], (int)g.map[c].size(), c, sup, ctx->stream));
-        nl[0]++;
+        nl[c]++;
       }
-    CK(cudaEventRecord(ev[3 * i + 1], ctx->stream));
-    CK(launch_post(ctx->d_ds, ctx->d_ch, ctx->d_post_map, ctx->post_blocks,
-                   false, sup, ctx->stream));
-    nl[1]++;
+    }
     nl[2]++;
     CK(cudaEventRecord(ev[3 * i + 2], ctx->stream));
   }
@@ -677,7 +707,7 @@ int64_t bsg_launches_per_sweep(const bsg_ctx *ctx) {
     if (std::find(ps.begin(), ps.end(), P) == ps.end()) ps.push_back(P);
   }
   ng = ps.size();
-  return (int64_t)(2 * ng + 1);
+  return (int64_t)(2 * ng);
 }
 
 void *bsg_stream(bsg_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
@@ -773,7 +803,7 @@ bsg_status bsg_get_sweep(bsg_ctx *ctx, int32_t chain, int64_t *sweep, int64_t *n
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaMemcpy(&h, counters_of(ctx->ch[chain]), sizeof(h), cudaMemcpyDeviceToHost));
-  if (sweep) *sweep = h.sweep;
+  if (sweep) *sweep = h.sweep[1];
   if (nkept) *nkept = h.nkept;
   return BSG_OK;
 }
@@ -902,27 +932,21 @@ bsg_status bsg_sweep_supplied(bsg_ctx *ctx, int32_t chain, const uint32_t *ubits
   sup.wnorm = dw;
   sup.form = form;
   // Block maps for this chain alone, one lane per voxel.
-  const int thr = 128;
-  std::vector<BlockMap> m[2], pm;
-  for (int col = 0; col < 2; ++col)
-    for (int st = 0; st < (int)d.vox[col].size(); st += thr)
-      m[col].push_back({chain, st});
-  const int per = kPostThreads * kPostPerThread;
-  for (int st = 0; st < d.V; st += per) pm.push_back({chain, st});
-  BlockMap *dm0 = upload(ctx, m[0].data(), m[0].size(), &e);
+  const int thr = kParityThreads;
+  std::vector<BlockMap> m[2];
+  for (int col = 0; col < 2; ++col) map_chain(m[col], chain, (int)d.vox[col].size(), thr, col);
+  e = cudaSuccess;
+  BlockMap *dm0 = m[0].empty() ? nullptr : upload(ctx, m[0].data(), m[0].size(), &e);
   CK(e);
   BlockMap *dm1 = upload(ctx, m[1].data(), m[1].size(), &e);
-  CK(e);
-  BlockMap *dpm = upload(ctx, pm.data(), pm.size(), &e);
   CK(e);
   CK(launch_fused(P, 1, thr, true, ctx->d_ds, ctx->d_ch, dm0, (int)m[0].size(), 0, sup,
                   ctx->stream));
   CK(launch_fused(P, 1, thr, true, ctx->d_ds, ctx->d_ch, dm1, (int)m[1].size(), 1, sup,
                   ctx->stream));
-  CK(launch_post(ctx->d_ds, ctx->d_ch, dpm, (int)pm.size(), true, sup, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   for (void *p : {(void *)du, (void *)dn, (void *)dc, (void *)dw, (void *)dm0,
-                  (void *)dm1, (void *)dpm})
+                  (void *)dm1})
     dfree(ctx, p);
   return bsg_sync(ctx);
 }

@@ -3,7 +3,9 @@
 // subjects from the packed outcome bits, accumulates X'(Z - b_WM WM) in
 // registers (Z never reaches memory), forms the conditional precision
 // Q = X'X + n_v Omega and mean vector, factors Q in registers and draws
-// beta_v.
+// beta_v.  With the new beta_v it also adds the kept sweep's FP64 running
+// sums and the column sums, and (colour 1) the voxel's Omega pair products;
+// the last colour-1 block of a chain draws Omega.  A sweep is two launches.
 //
 // Replaces Z_GPU1 (covarGPU.cu:1368-1428) + Spat_Coef_Probit
 // (covarGPU.cu:293-396) and the CPU updateZ / Spat_Coefff
@@ -17,7 +19,7 @@
 // memory, so one Philox call serves four consecutive subjects of one lane.
 #pragma once
 
-#include "bsg_device.cuh"
+#include "bsg_wishart.cuh"
 
 namespace bsg {
 
@@ -52,13 +54,13 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
   const int j = bm.start + g;
   const bool active = j < nc;
   const int N = d.N, Vp = d.Vp;
-  const uint32_t sweep = (uint32_t)(*ch.sweep);
+  // This colour's own sweep counter: the previous launch of this colour
+  // finished before this one started (see the dependency protocol below).
+  const long long sweep_ll = ch.sweep[colour];
+  const uint32_t sweep = (uint32_t)sweep_ll;
   const uint32_t cid = ch.chain_id << 8;
-
-  for (int t = tid; t < P * P; t += blockDim.x) {
-    Om[t] = ch.omega_f[t];
-    Xtx[t] = d.xtx[t];
-  }
+  const bool kept =
+      sweep_ll > ch.burnin && (sweep_ll % (ch.thin > 0 ? ch.thin : 1)) == 0;
 
   float beta[P], acc[P];
   int v = 0, sc = 0;
@@ -159,100 +161,267 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
       for (int o = LPV / 2; o > 0; o >>= 1)
         acc[p] += __shfl_xor_sync(0xffffffffu, acc[p], o);
   }
-  if (!active || k != 0) {
-    if (!ok) atomicOr(ch.status, kErrTnCap);
+
+  // ---- dependency protocol (programmatic dependent launch) --------------
+  // Everything above read only this colour's own coefficients, the design
+  // and the outcome bits, all final since this colour's previous launch.
+  // The beta update needs Omega and the other colour's new coefficients,
+  // written by the previous kernel in the stream: wait for its completion
+  // here, and only then let the next kernel start its own latent phase.
+  // (Without a programmatic launch both calls return at once.)
+  cudaGridDependencySynchronize();
+  cudaTriggerProgrammaticLaunchCompletion();
+  const long long nk = *ch.nkept;
+  for (int t = tid; t < P * P; t += blockDim.x) {
+    Om[t] = ch.omega_f[t];
+    Xtx[t] = d.xtx[t];
+  }
+  __syncthreads();
+  const bool leader = active && k == 0;
+  int err = ok ? 0 : kErrTnCap;
+  float bnew[P];   // the voxel's coefficients at the end of the sweep
+  float pv[NT];    // its Omega pair products (colour 1)
+#pragma unroll
+  for (int p = 0; p < P; ++p) bnew[p] = beta[p];
+#pragma unroll
+  for (int q = 0; q < NT; ++q) pv[q] = 0.f;
+
+  if (leader) {
+    // ---- beta_v | rest  (Spat_Coefff, covar.cpp:142-180) ---------------
+    float sumV[P];
+#pragma unroll
+    for (int p = 0; p < P; ++p) sumV[p] = 0.f;
+#pragma unroll
+    for (int t = 1; t <= 6; ++t) {
+      const int sn = d.nb[colour][(size_t)t * nc + j];
+#pragma unroll
+      for (int p = 0; p < P; ++p) sumV[p] += ch.beta[(size_t)p * Vp + sn];
+    }
+    const unsigned nbm = d.nbm[colour][j];
+    const float nnb = (float)__popc(nbm);
+    float b[P], Q[NT];
+#pragma unroll
+    for (int a = 0; a < P; ++a) {
+      float s = acc[a];
+#pragma unroll
+      for (int q = 0; q < P; ++q) s += Om[q + a * P] * sumV[q];
+      b[a] = s;
+#pragma unroll
+      for (int q = 0; q <= a; ++q) Q[tri(a, q)] = Xtx[q + a * P] + nnb * Om[q + a * P];
+    }
+    bool okc = chol_packed<P>(Q);
+
+    float e[P];
+    if (SUPP) {
+#pragma unroll
+      for (int p = 0; p < P; ++p) e[p] = __ldg(sup.normals + (size_t)v * P + p);
+    } else {
+#pragma unroll
+      for (int p0 = 0; p0 < P; p0 += 4) {
+        const uint4 r = philox(make_uint4((uint32_t)(p0 >> 2), (uint32_t)v, sweep,
+                                          cid | kTagBeta), key);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (p0 + q < P) e[p0 + q] = normal_of(pick4(r, q));
+      }
+    }
+
+    float out[P];
+    if (!SUPP || sup.form == 1) {
+      // Q = G G':  m = G^-T G^-1 b,  beta = m + G^-T e = G^-T (G^-1 b + e)
+      solve_lower<P>(Q, b);
+#pragma unroll
+      for (int p = 0; p < P; ++p) out[p] = b[p] + e[p];
+      solve_upper<P>(Q, out);
+    } else {
+      // Reference draw (covar.cpp:168-177): V = Q^-1 by columns
+      // (cholesky_invert_float), m = V b, L = chol(V), beta = m + L e.
+      float Vc[P][P];  // Vc[k][q] = entry q of column k of Q^-1
+#pragma unroll
+      for (int kk = 0; kk < P; ++kk) {
+        float x[P];
+#pragma unroll
+        for (int q = 0; q < P; ++q) x[q] = (q == kk) ? 1.f : 0.f;
+        solve_lower<P>(Q, x);
+        solve_upper<P>(Q, x);
+#pragma unroll
+        for (int q = 0; q < P; ++q) Vc[kk][q] = x[q];
+      }
+      float m[P], L[NT];
+#pragma unroll
+      for (int a = 0; a < P; ++a) {
+        float s = 0.f;
+#pragma unroll
+        for (int q = 0; q < P; ++q) s += Vc[a][q] * b[q];
+        m[a] = s;
+#pragma unroll
+        for (int q = 0; q <= a; ++q) L[tri(a, q)] = Vc[a][q];
+      }
+      okc = chol_packed<P>(L) && okc;
+#pragma unroll
+      for (int a = 0; a < P; ++a) {
+        float s = 0.f;
+#pragma unroll
+        for (int q = 0; q <= a; ++q) s += L[tri(a, q)] * e[q];
+        out[a] = s + m[a];
+      }
+    }
+
+    bool fin = true;
+#pragma unroll
+    for (int p = 0; p < P; ++p) fin = fin && isfinite(out[p]);
+    if (okc && fin) {
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        ch.beta[(size_t)p * Vp + sc] = out[p];
+        bnew[p] = out[p];
+      }
+    }
+    err |= (okc ? 0 : kErrChol) | ((okc && !fin) ? kErrNaN : 0);
+
+    // ---- posterior running sums of the kept sweep (mcmc.cpp:637-645) --
+    if (kept) {
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        const double x = (double)bnew[p];
+        ch.acc_sum[(size_t)p * d.V + v] += x;
+        ch.acc_sq[(size_t)p * d.V + v] += x * x;
+      }
+#pragma unroll
+      for (int g2 = 0; g2 < P; ++g2)
+        if (g2 < d.S)
+          ch.prb_sum[(size_t)g2 * d.V + v] += (double)prob_sdnorm(bnew[g2] + bwm);
+    }
+
+    // ---- Omega pair products (Spat_Coef_Prec, covarGPU.cu:953-1013) -----
+    // Every in-mask edge joins a colour-0 and a colour-1 voxel, so the
+    // colour-1 pass sees each edge once.  For a forward neighbour (+x, +y,
+    // +z) the reference tests the neighbour's row coefficient; for a
+    // backward one the edge is counted when that neighbour is in the mask
+    // and this voxel's row coefficient is nonzero (covar.cpp:235-253).
+    if (colour == 1) {
+#pragma unroll
+      for (int t = 0; t < 6; ++t) {
+        const int sn = d.nb[1][(size_t)(t + 1) * nc + j];
+        const bool fwd = t & 1;
+        const bool nin = (nbm >> t) & 1u;
+        float dd[P];
+        bool ind[P];
+#pragma unroll
+        for (int p = 0; p < P; ++p) {
+          const float bn = ch.beta[(size_t)p * Vp + sn];
+          dd[p] = bnew[p] - bn;
+          ind[p] = fwd ? (bn != 0.f) : (nin && bnew[p] != 0.f);
+        }
+#pragma unroll
+        for (int r = 0; r < P; ++r)
+          if (ind[r]) {
+#pragma unroll
+            for (int c2 = 0; c2 <= r; ++c2) pv[tri(r, c2)] += dd[r] * dd[c2];
+          }
+      }
+    }
+  } else {
+#pragma unroll
+    for (int p = 0; p < P; ++p) bnew[p] = 0.f;  // no column-sum share
+  }
+  if (err) atomicOr(ch.status, err);
+
+  // ---- block partials: column sums (both colours) and pairs (colour 1) --
+  __shared__ double red[kMaxThreads / 32][kPostVals];
+  __shared__ double tot[kPostVals];
+  __shared__ int is_last;
+  const int lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+  constexpr int kColOff = kMaxPairs;
+#pragma unroll
+  for (int q = 0; q < NT + P; ++q) {
+    if (colour == 0 && q < NT) continue;
+    double val = q < NT ? (double)pv[q] : (double)bnew[q - NT];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+    if (lane == 0) red[warp][q < NT ? q : kColOff + (q - NT)] = val;
+  }
+  __syncthreads();
+  const int vpb = blockDim.x / LPV;
+  const int lb = bm.start / vpb;
+  if (colour == 0) {
+    if (tid < P) {
+      double s = 0.0;
+      for (int w = 0; w < nwarp; ++w) s += red[w][kColOff + tid];
+      ch.partials0[(size_t)lb * kMaxP + tid] = s;
+      __threadfence();
+    }
+    __syncthreads();
+    if (tid == 0) {  // the last colour-0 block advances this colour's count
+      const int nblk0 = (nc + vpb - 1) / vpb;
+      if (atomicAdd(ch.done, 1u) == (unsigned)(nblk0 - 1)) {
+        ch.sweep[0] = sweep_ll + 1;
+        ch.done[0] = 0u;
+        __threadfence();
+      }
+    }
     return;
   }
-
-  // ---- beta_v | rest  (Spat_Coefff, covar.cpp:142-180) -----------------
-  float sumV[P];
-#pragma unroll
-  for (int p = 0; p < P; ++p) sumV[p] = 0.f;
-#pragma unroll
-  for (int t = 1; t <= 6; ++t) {
-    const int sn = d.nb[colour][(size_t)t * nc + j];
-#pragma unroll
-    for (int p = 0; p < P; ++p) sumV[p] += ch.beta[(size_t)p * Vp + sn];
+  if (tid < kPostVals) {
+    const bool live = tid < kMaxPairs ? tid < NT : (tid - kColOff) < P;
+    double s = 0.0;
+    if (live)
+      for (int w = 0; w < nwarp; ++w) s += red[w][tid];
+    ch.partials1[(size_t)lb * kPostVals + tid] = s;
+    __threadfence();
   }
-  const float nnb = (float)d.nnb[colour][j];
-  float b[P], Q[NT];
-#pragma unroll
-  for (int a = 0; a < P; ++a) {
-    float s = acc[a];
-#pragma unroll
-    for (int q = 0; q < P; ++q) s += Om[q + a * P] * sumV[q];
-    b[a] = s;
-#pragma unroll
-    for (int q = 0; q <= a; ++q) Q[tri(a, q)] = Xtx[q + a * P] + nnb * Om[q + a * P];
+  __syncthreads();
+  const int nblk1 = max(1, (nc + vpb - 1) / vpb);
+  if (tid == 0) {
+    const unsigned prev = atomicAdd(ch.done + 1, 1u);
+    is_last = prev == (unsigned)(nblk1 - 1);
   }
-  bool okc = chol_packed<P>(Q);
-
-  float e[P];
-  if (SUPP) {
-#pragma unroll
-    for (int p = 0; p < P; ++p) e[p] = __ldg(sup.normals + (size_t)v * P + p);
-  } else {
-#pragma unroll
-    for (int p0 = 0; p0 < P; p0 += 4) {
-      const uint4 r = philox(make_uint4((uint32_t)(p0 >> 2), (uint32_t)v, sweep,
-                                        cid | kTagBeta), key);
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        if (p0 + q < P) e[p0 + q] = normal_of(pick4(r, q));
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  // Sum the partial rows in block order (fixed, so the draw is bitwise
+  // reproducible): warp w takes values q = w, w + nwarp, ...
+  const int n0 = d.n[0];
+  const int nblk0 = (n0 + vpb - 1) / vpb;
+  for (int q = warp; q < kPostVals; q += nwarp) {
+    const bool live = q < kMaxPairs ? q < NT : (q - kColOff) < P;
+    double s = 0.0;
+    if (live) {
+      for (int bb = lane; bb < nblk1; bb += 32)
+        s += __ldcg(ch.partials1 + (size_t)bb * kPostVals + q);
+      if (q >= kColOff)
+        for (int bb = lane; bb < nblk0; bb += 32)
+          s += __ldcg(ch.partials0 + (size_t)bb * kMaxP + (q - kColOff));
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) tot[q] = s;
   }
+  __syncthreads();
+  if (warp == 0)
+    wishart_warp(ch, d, tot, (long long)sweep_ll, kept, nk, SUPP ? 1 : 0, sup, lane);
+}
 
-  float out[P];
-  if (!SUPP || sup.form == 1) {
-    // Q = G G':  m = G^-T G^-1 b,  beta = m + G^-T e = G^-T (G^-1 b + e)
-    solve_lower<P>(Q, b);
-#pragma unroll
-    for (int p = 0; p < P; ++p) out[p] = b[p] + e[p];
-    solve_upper<P>(Q, out);
-  } else {
-    // Reference draw (covar.cpp:168-177): V = Q^-1 by columns
-    // (cholesky_invert_float), m = V b, L = chol(V), beta = m + L e.
-    float Vc[P][P];  // Vc[k][q] = entry q of column k of Q^-1
-#pragma unroll
-    for (int kk = 0; kk < P; ++kk) {
-      float x[P];
-#pragma unroll
-      for (int q = 0; q < P; ++q) x[q] = (q == kk) ? 1.f : 0.f;
-      solve_lower<P>(Q, x);
-      solve_upper<P>(Q, x);
-#pragma unroll
-      for (int q = 0; q < P; ++q) Vc[kk][q] = x[q];
-    }
-    float m[P], L[NT];
-#pragma unroll
-    for (int a = 0; a < P; ++a) {
-      float s = 0.f;
-#pragma unroll
-      for (int q = 0; q < P; ++q) s += Vc[a][q] * b[q];
-      m[a] = s;
-#pragma unroll
-      for (int q = 0; q <= a; ++q) L[tri(a, q)] = Vc[a][q];
-    }
-    okc = chol_packed<P>(L) && okc;
-#pragma unroll
-    for (int a = 0; a < P; ++a) {
-      float s = 0.f;
-#pragma unroll
-      for (int q = 0; q <= a; ++q) s += L[tri(a, q)] * e[q];
-      out[a] = s + m[a];
-    }
-  }
-
-  bool fin = true;
-#pragma unroll
-  for (int p = 0; p < P; ++p) fin = fin && isfinite(out[p]);
-  if (okc && fin) {
-#pragma unroll
-    for (int p = 0; p < P; ++p) ch.beta[(size_t)p * Vp + sc] = out[p];
-  }
-  const int err = (ok ? 0 : kErrTnCap) | (okc ? 0 : kErrChol) |
-                  ((okc && !fin) ? kErrNaN : 0);
-  if (err) atomicOr(ch.status, err);
+// Launch of one instantiation; with pdl the launch carries the
+// programmatic-stream-serialization attribute, so it may start once every
+// block of the previous kernel in the stream has passed its dependency
+// point.
+template <int P, int LPV, bool SUPP>
+cudaError_t launch_one(int nblocks, int threads, cudaStream_t st, bool pdl,
+                       const DatasetDev *ds, ChainDev *ch, const BlockMap *map,
+                       int colour, const Supplied &sup) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(nblocks);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, fused_colour_kernel<P, LPV, SUPP>, ds, ch, map,
+                            colour, sup);
 }
 
 // Instantiation helper used by bsg_fused_l*.cu.
@@ -260,19 +429,18 @@ template <int LPV>
 cudaError_t launch_fused_lpv(int P, int threads, bool supplied,
                              const DatasetDev *ds, ChainDev *ch,
                              const BlockMap *map, int nblocks, int colour,
-                             const Supplied &sup, cudaStream_t st) {
+                             const Supplied &sup, cudaStream_t st, bool pdl) {
   if (nblocks <= 0) return cudaSuccess;
+  cudaError_t e = cudaErrorInvalidValue;
 #define BSG_CASE(PP)                                                        \
   case PP:                                                                  \
     if (supplied) {                                                         \
       if constexpr (LPV == 1)                                               \
-        fused_colour_kernel<PP, LPV, true>                                  \
-            <<<nblocks, threads, 0, st>>>(ds, ch, map, colour, sup);        \
-      else                                                                  \
-        return cudaErrorInvalidValue;                                       \
+        e = launch_one<PP, LPV, true>(nblocks, threads, st, pdl, ds, ch,    \
+                                      map, colour, sup);                    \
     } else {                                                                \
-      fused_colour_kernel<PP, LPV, false>                                   \
-          <<<nblocks, threads, 0, st>>>(ds, ch, map, colour, sup);          \
+      e = launch_one<PP, LPV, false>(nblocks, threads, st, pdl, ds, ch,     \
+                                     map, colour, sup);                     \
     }                                                                       \
     break;
   switch (P) {
@@ -288,7 +456,7 @@ cudaError_t launch_fused_lpv(int P, int threads, bool supplied,
       return cudaErrorInvalidValue;
   }
 #undef BSG_CASE
-  return cudaGetLastError();
+  return e;
 }
 
 }  // namespace bsg

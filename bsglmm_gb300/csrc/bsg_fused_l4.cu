@@ -7,8 +7,8 @@ namespace bsg {
 cudaError_t launch_fused_l4(int P, int threads, bool supplied,
                             const DatasetDev *ds, ChainDev *ch,
                             const BlockMap *map, int nblocks, int colour,
-                            const Supplied &sup, cudaStream_t st) {
+                            const Supplied &sup, cudaStream_t st, bool pdl) {
   return launch_fused_lpv<4>(P, threads, supplied, ds, ch, map, nblocks,
-                              colour, sup, st);
+                              colour, sup, st, pdl);
 }
 }  // namespace bsg

@@ -16,8 +16,9 @@ constexpr int kChunkPad = kChunk + kChunk / 32;     // one pad word per 32
 constexpr float kATail = 5.0f;  // inversion below, rejection above
 constexpr int kTailMax = 16;    // rejection attempts per latent draw
 constexpr int kGammaMax = 64;   // Marsaglia-Tsang attempts per gamma draw
-constexpr int kPostThreads = 256;
-constexpr int kPostPerThread = 4;
+constexpr int kPostThreads = 256;   // block shape of the allocation-free
+constexpr int kPostPerThread = 4;   // Omega pass (bsg_noalloc.cu)
+constexpr int kMaxThreads = 256;    // largest block of the colour kernel
 
 // Philox counter tags: c3 = chain << 8 | tag.
 enum : uint32_t {
@@ -47,7 +48,7 @@ struct DatasetDev {
   const float *wm;             // [V] or nullptr (WM = 1)
   const int32_t *nb[2];        // [7][n_c]: sc(self), sc of the 6 neighbours
                                // in the order -x, +x, -y, +y, -z, +z
-  const uint8_t *nnb[2];       // [n_c] in-mask neighbour count
+  const uint8_t *nbm[2];       // [n_c] bit t set iff neighbour t is in mask
   const int32_t *vidx[2];      // [n_c] compact mask index
   const uint32_t *ybits[2];    // [W][n_c] outcome bits, bit b = subject 32w+b
 };
@@ -58,7 +59,6 @@ struct ChainDev {
   uint32_t key0, key1, chain_id;
   float beta_wm;
   int32_t df_offset, burnin, thin;
-  int32_t post_blocks;     // blocks of the post-sweep kernel for this chain
   float *beta;             // [P][Vp]
   float *omega_f;          // [P*P] float copy read by the colour kernels
   double *omega_d;         // [P*P]
@@ -66,9 +66,11 @@ struct ChainDev {
   double *acc_sum;         // [P][V]  sum of beta over kept sweeps
   double *acc_sq;          // [P][V]  sum of beta^2
   double *prb_sum;         // [S][V]  sum of the lesion probability
-  double *partials;        // [post_blocks][kPostVals]
-  unsigned int *done;      // arrival counter of the post-sweep kernel
-  long long *sweep;        // index of the sweep being drawn
+  double *partials0;       // [colour-0 blocks][kMaxP] column sums
+  double *partials1;       // [colour-1 blocks][kPostVals] pairs + column sums
+  unsigned int *done;      // [2] arrival counters of the colour kernels
+  long long *sweep;        // [2] sweeps completed by the colour-c kernel;
+                           // sweep[1] is the chain's completed-sweep count
   long long *nkept;        // kept sweeps accumulated
   int *status;             // sticky error bits
 };
@@ -91,10 +93,8 @@ struct BlockMap {
 cudaError_t launch_fused(int P, int lpv, int threads, bool supplied,
                          const DatasetDev *ds, ChainDev *ch,
                          const BlockMap *map, int nblocks, int colour,
-                         const Supplied &sup, cudaStream_t st);
-cudaError_t launch_post(const DatasetDev *ds, ChainDev *ch,
-                        const BlockMap *map, int nblocks, bool supplied,
-                        const Supplied &sup, cudaStream_t st);
+                         const Supplied &sup, cudaStream_t st,
+                         bool pdl = false);
 cudaError_t launch_prb(const DatasetDev *ds, const ChainDev *ch, int chain,
                        const DatasetDev &dh, float *prb, cudaStream_t st);
 cudaError_t launch_pack(const uint8_t *bytes, int N, int V, int nc,

@@ -1,0 +1,166 @@
+// bsg_wishart.cuh -- the FP64 Omega | beta draw run by one warp at the end
+// of a sweep: Marsaglia-Tsang gamma variates, warp-parallel Cholesky, and
+// the Bartlett construction.
+#pragma once
+
+#include "bsg_device.cuh"
+
+namespace bsg {
+
+// ----------------------------------------------------- FP64 Wishart tail --
+// Marsaglia & Tsang (2000) gamma(a, 1); a < 1 through the U^(1/a) boost.
+// Attempt t of slot uses counter (slot*64 + t, 0, sweep, chain<<8|GAMMA).
+static __device__ double gamma_mt(double a, uint32_t slot, uint32_t sweep,
+                                  uint32_t c3, uint32_t k0, uint32_t k1,
+                                  int *err) {
+  const bool boost = a < 1.0;
+  const double aa = boost ? a + 1.0 : a;
+  const double dd = aa - 1.0 / 3.0, c = 1.0 / sqrt(9.0 * dd);
+  for (int t = 0; t < kGammaMax; ++t) {
+    const uint4 r = philox1(make_uint4(slot * 64u + (uint32_t)t, 0u, sweep, c3),
+                            k0, k1);
+    const double x = (double)normal_of(r.x);
+    const double cx = c * x;
+    if (!(cx > -1.0)) continue;
+    const double v3 = (1.0 + cx) * (1.0 + cx) * (1.0 + cx);
+    const double lhs = log(u_of_d(r.y));
+    const double rhs = 0.5 * x * x + dd * (1.0 - v3 + 3.0 * log1p(cx));
+    if (lhs < rhs) return dd * v3 * (boost ? pow(u_of_d(r.z), 1.0 / a) : 1.0);
+  }
+  *err |= kErrGammaCap;
+  return dd;
+}
+
+// In-place Cholesky of the lower triangle of the P x P matrix A (row-major
+// A[r*kMaxP + c]) by one warp, rows across lanes (the outer-product scheme
+// of cholesky.cpp:13-33).  Returns false (warp-uniform) on a non-positive
+// pivot.
+static __device__ bool chol_warp(double (*A)[kMaxP], int P, int lane) {
+  bool ok = true;
+  for (int k = 0; k < P; ++k) {
+    const double d = A[k][k];
+    ok = ok && (d > 0.0);
+    const double s = sqrt(d);
+    __syncwarp();
+    if (lane == k) A[k][k] = s;
+    if (lane > k && lane < P) A[lane][k] /= s;
+    __syncwarp();
+    if (lane > k && lane < P)
+      for (int j = k + 1; j <= lane; ++j) A[lane][j] -= A[lane][k] * A[j][k];
+    __syncwarp();
+  }
+  return ok;
+}
+
+// Omega | beta ~ Wishart(df, (S + I)^-1) by the Bartlett construction of
+// rwishart2 (cholesky.cpp:245-286) after chol -> invert -> chol
+// (covar.cpp:286-291, covarGPU.cu:1099-1104), FP64, one warp.
+static __device__ void wishart_warp(const ChainDev &ch, const DatasetDev &d,
+                                    const double *tot, long long sweep,
+                                    bool kept, long long nk, int supplied,
+                                    const Supplied &sup, int lane) {
+  __shared__ double A[kMaxP][kMaxP], Ai[kMaxP][kMaxP], T[kMaxP][kMaxP],
+      B[kMaxP][kMaxP];
+  const int P = d.P;
+  int err = 0;
+  if (lane < P)
+    for (int c = 0; c < P; ++c) {
+      const int r = lane;
+      A[r][c] = (r >= c ? tot[tri(r, c)] : tot[tri(c, r)]) + (r == c ? 1.0 : 0.0);
+      T[r][c] = 0.0;
+    }
+  __syncwarp();
+  bool ok = chol_warp(A, P, lane);
+  if (ok) {
+    // column `lane` of (G G')^-1 by forward then back substitution
+    if (lane < P) {
+      double col[kMaxP];
+      for (int i = 0; i < P; ++i) col[i] = (i == lane) ? 1.0 : 0.0;
+      for (int i = 0; i < P; ++i) {
+        double s = 0.0;
+        for (int j = 0; j < i; ++j) s += A[i][j] * col[j];
+        col[i] = (col[i] - s) / A[i][i];
+      }
+      for (int i = P - 1; i >= 0; --i) {
+        double s = 0.0;
+        for (int j = i + 1; j < P; ++j) s += A[j][i] * col[j];
+        col[i] = (col[i] - s) / A[i][i];
+      }
+      for (int i = 0; i < P; ++i) Ai[lane][i] = col[i];  // row `lane` of Ai
+    }
+    __syncwarp();
+    ok = chol_warp(Ai, P, lane);
+  }
+  if (ok) {
+    const double df = (double)d.V + (double)ch.df_offset;
+    const uint32_t cid = ch.chain_id << 8, sw = (uint32_t)sweep;
+    if (lane < P) {
+      const double c2 = supplied ? sup.chi2[lane]
+                                 : 2.0 * gamma_mt(0.5 * (df - lane), (uint32_t)lane,
+                                                  sw, cid | kTagGamma, ch.key0,
+                                                  ch.key1, &err);
+      T[lane][lane] = sqrt(c2);
+    }
+    const int nw = P * (P - 1) / 2;
+    if (lane < nw) {
+      int i = 1;
+      while ((i + 1) * i / 2 <= lane) ++i;  // row i: lane in [i(i-1)/2, i(i+1)/2)
+      const int j = lane - i * (i - 1) / 2;
+      double z;
+      if (supplied) {
+        z = sup.wnorm[lane];
+      } else {
+        const uint4 r = philox1(make_uint4((uint32_t)(lane >> 2), 0u, sw,
+                                           cid | kTagWNorm),
+                                ch.key0, ch.key1);
+        z = (double)normal_of(pick4(r, lane & 3));
+      }
+      T[i][j] = z;
+    }
+    __syncwarp();
+    if (lane < P) {  // row `lane` of B = L T (L lower from Ai)
+      const int i = lane;
+      for (int j = 0; j < P; ++j) {
+        double s = 0.0;
+        for (int k = j; k <= i; ++k) s += Ai[i][k] * T[k][j];
+        B[i][j] = j <= i ? s : 0.0;
+      }
+    }
+    __syncwarp();
+    bool fin = true;
+    if (lane < P) {
+      const int i = lane;
+      for (int j = 0; j < P; ++j) {
+        const int K = i < j ? i : j;
+        double s = 0.0;
+        for (int k = 0; k <= K; ++k) s += B[i][k] * B[j][k];
+        A[i][j] = s;  // A is free again
+        fin = fin && isfinite(s);
+      }
+    }
+    fin = __all_sync(0xffffffffu, fin);
+    __syncwarp();
+    if (fin) {
+      if (lane < P)
+        for (int j = 0; j < P; ++j) {
+          ch.omega_d[lane * P + j] = A[lane][j];
+          ch.omega_f[lane * P + j] = (float)A[lane][j];
+        }
+    } else {
+      err |= kErrNaN;
+    }
+  } else {
+    err |= kErrWishart;
+  }
+  if (lane < P) ch.colmean[lane] = (float)(tot[kMaxPairs + lane] / (double)d.V);
+  err = __reduce_or_sync(0xffffffffu, err);
+  if (lane == 0) {
+    if (err) atomicOr(ch.status, err);
+    ch.sweep[1] = sweep + 1;
+    if (kept) *ch.nkept = nk + 1;
+    ch.done[1] = 0u;
+    __threadfence();
+  }
+}
+
+}  // namespace bsg

@@ -86,8 +86,8 @@ bsg_status bsg_add_dataset(bsg_ctx *ctx, const bsg_dataset_desc *desc,
 /* Adds a chain with beta = 0 and Omega = I (mcmc.cpp:149-154,227). */
 bsg_status bsg_add_chain(bsg_ctx *ctx, int32_t dataset_id,
                          const bsg_chain_desc *desc, int32_t *chain_id);
-/* Tile shape of the fused colour kernel: lanes per voxel (1,2,4,8,16,32)
- * and threads per block (64..1024); 0 keeps the current choice. */
+/* Tile shape of the fused colour kernel: lanes per voxel (1, 2, 4, 8) and
+ * threads per block (64, 128, 256); 0 keeps the current choice. */
 bsg_status bsg_set_tuning(bsg_ctx *ctx, int32_t lanes_per_voxel,
                           int32_t block_threads);
 bsg_status bsg_get_tuning(const bsg_ctx *ctx, int32_t *lanes_per_voxel,
@@ -104,8 +104,8 @@ bsg_status bsg_sync(bsg_ctx *ctx);
  * context's stream around the whole batch). */
 bsg_status bsg_run_timed(bsg_ctx *ctx, int64_t nsweeps, double *ms);
 /* Runs nsweeps without graphs with CUDA events around each kernel class:
- * ms[0] fused colour kernels, ms[1] Omega/accumulator pass (including the
- * Wishart tail), ms[2] whole sweeps.  launches[0..2] counts. */
+ * ms[0] colour-0 kernels, ms[1] colour-1 kernels (which also reduce the
+ * Omega pairs and draw Omega), ms[2] whole sweeps; launches[0..2] counts. */
 bsg_status bsg_profile(bsg_ctx *ctx, int64_t nsweeps, double *ms,
                        int64_t *launches);
 /* Kernel launches issued per sweep by bsg_run (for launch accounting). */

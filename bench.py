@@ -195,6 +195,21 @@ def flush_l2(buf):
     buf.zero_()
 
 
+def reduce_max(x: float, world: int) -> float:
+    """Max over ranks (the slowest replica sets the job's time)."""
+    if world > 1:
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+    return float(x)
+
+
+def chain_seed(rank: int) -> int:
+    """Each replica runs an independent chain."""
+    return 1 + rank
+
+
 def run_ours(args, rank, world, local):
     import torch
     import bsglmm_gb300 as bsg
@@ -208,7 +223,7 @@ def run_ours(args, rank, world, local):
     N, P, S, V = study.N, study.P, study.nsubtypes, study.V
     s = bsg.Sampler(local)
     ds = s.add_dataset(study.mask, study.covar, study.data, S)
-    ch = s.add_chain(ds, seed=1 + rank, burnin=0, thin=1)
+    ch = s.add_chain(ds, seed=chain_seed(rank), burnin=0, thin=1)
     if args.lpv or args.threads:
         s.set_tuning(args.lpv, args.threads)
     lpv, thr = s.tuning()
@@ -236,11 +251,7 @@ def run_ours(args, rank, world, local):
         s.sync()
         wall = time.perf_counter() - t0
     barrier()
-    total_ms = float(sum(dev_ms))
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = reduce_max(sum(dev_ms), world)
     ms_per_step = total_ms / args.steps
     value = world * N * V * args.steps / (total_ms * 1e-3)
 
@@ -256,11 +267,7 @@ def run_ours(args, rank, world, local):
         om = s.omega(ch)
         _ = s.colmeans(ch)
     s.sync()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = reduce_max(time.perf_counter() - t0, world)
     e2e = world * N * V * args.steps / e2e_s
 
     # live per-kernel timing of the same sweep (CUDA events on the sampler's
@@ -322,6 +329,97 @@ def run_ours(args, rank, world, local):
     s.close()
 
 
+# ------------------------------------------------- batched workloads ---
+BATCHED = {
+    "c0": "64 chains of the 20^3 sphere study (N=50, P=3) in one context",
+    "c3": "64 replicate studies (cube side 32-64, N 40-400, P 2-6) in one context",
+    "c4": "16 chains on a 182x218x182 ellipsoid (1.5M voxels, N=500, P=6)",
+}
+
+
+def batched_workload(name):
+    from bsglmm_gb300 import synth
+    if name == "c0":
+        return [synth.config0(0)], [64]
+    if name == "c3":
+        sts = synth.config3()
+        return sts, [1] * len(sts)
+    if name == "c4":
+        return [synth.config4()], [16]
+    raise ValueError(name)
+
+
+def run_batched(args, rank, world, local):
+    """Throughput of one context holding every chain of the workload (one
+    batched launch per P group and colour) against the plain form: each
+    single-chain study in its own context, swept one after another with a
+    synchronisation per sweep.  Wall time per sweep, L2 flushed between
+    sweeps."""
+    import torch
+    import bsglmm_gb300 as bsg
+    torch.cuda.set_device(local)
+    studies, nchains = batched_workload(args.workload)
+    upd = sum(st.N * st.V * c for st, c in zip(studies, nchains))
+    flushbuf = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def timed(samplers, steps):
+        ts = []
+        for _ in range(steps):
+            flush_l2(flushbuf)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for smp in samplers:
+                smp.run(1, sync=len(samplers) > 1)
+            for smp in samplers:
+                smp.sync()
+            ts.append(time.perf_counter() - t0)
+        return float(np.median(ts))
+
+    batched = bsg.Sampler(local)
+    for k, (st, nc) in enumerate(zip(studies, nchains)):
+        ds = batched.add_dataset(st.mask, st.covar, st.data, st.nsubtypes)
+        for c in range(nc):
+            batched.add_chain(ds, seed=1000 * k + c + 1)
+    for _ in range(args.warmup):
+        batched.run(1)
+    with Clocks(local) as clk:
+        t_b = timed([batched], args.steps)
+    launches = batched.launches_per_sweep()
+    batched.close()
+    plain = None
+    if args.workload in ("c0", "c3"):
+        sams = []
+        for k, (st, nc) in enumerate(zip(studies, nchains)):
+            for c in range(nc):
+                smp = bsg.Sampler(local)
+                d = smp.add_dataset(st.mask, st.covar, st.data, st.nsubtypes)
+                smp.add_chain(d, seed=1000 * k + c + 1)
+                sams.append(smp)
+        for smp in sams:
+            smp.run(args.warmup)
+        t_p = timed(sams, max(3, args.steps // 10))
+        for smp in sams:
+            smp.close()
+        plain = {"value": upd / t_p, "ms_per_sweep": t_p * 1e3,
+                 "contexts": len(sams), "launches_per_sweep": 2 * len(sams)}
+    line = {
+        "metric": METRIC, "value": upd / t_b, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_b * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (f64 Omega/accumulators)", "data": "synthetic",
+        "config": {"workload": BATCHED[args.workload], "studies": len(studies),
+                   "chains": sum(nchains), "updates_per_sweep": upd,
+                   "voxels": sum(st.V for st in studies),
+                   "l2": "flushed between timed sweeps", "timing": "wall, median"},
+        "sweeps_per_s": 1.0 / t_b, "gpu_launches_per_sweep": launches,
+        "plain": plain,
+        "batched_over_plain": (upd / t_b) / plain["value"] if plain else None,
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -331,8 +429,12 @@ def main():
     ap.add_argument("--lpv", type=int, default=0)
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="brain", choices=["brain"] + sorted(BATCHED))
     args = ap.parse_args()
     rank, world, local = dist_env()
+    if args.workload != "brain" and args.impl == "ours":
+        run_batched(args, rank, world, local)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
     else:

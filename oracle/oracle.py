@@ -216,7 +216,8 @@ class Problem:
         with np.errstate(invalid="ignore", divide="ignore"):
             mean = s1 / T
             var = (s2 - T * mean * mean) / (T - 1)
-        return dict(beta=b, omega=om, mean=mean, var=var, prb=sp[: self.S] / T,
+            prb = sp[: self.S] / T
+        return dict(beta=b, omega=om, mean=mean, var=var, prb=prb,
                     sum=s1, sumsq=s2, nkept=T, err=err)
 
 

@@ -47,6 +47,7 @@ SIGNATURES = {
     "bsg_get_omega": (_i32, [_P, _i32, _P]),
     "bsg_set_omega": (_i32, [_P, _i32, _P]),
     "bsg_get_colmeans": (_i32, [_P, _i32, _P]),
+    "bsg_set_beta_wm": (_i32, [_P, _i32, C.c_float]),
     "bsg_get_sweep": (_i32, [_P, _i32, C.POINTER(_i64), C.POINTER(_i64)]),
     "bsg_compute_prb": (_i32, [_P, _i32, _P]),
     "bsg_get_posterior": (_i32, [_P, _i32, _P, _P, _P, C.POINTER(_i64)]),
@@ -54,6 +55,10 @@ SIGNATURES = {
     "bsg_reset_accumulators": (_i32, [_P, _i32]),
     "bsg_sweep_supplied": (_i32, [_P, _i32, _P, _P, _P, _P, _i32]),
     "bsg_fp32_peak": (_i32, [_i32, C.POINTER(C.c_double)]),
+    "bsg_checkpoint_size": (_i64, [_P, _i32]),
+    "bsg_checkpoint": (_i32, [_P, _i32, _P, _i64]),
+    "bsg_restore": (_i32, [_P, _i32, _P, _i64]),
+    "bsg_autotune": (_i32, [_P, _i32, C.POINTER(_i32), C.POINTER(_i32)]),
     "bsg_omega_update_noalloc": (_i32, [_P, _P, _P, _i32, _i32, _i32, _i32, _i32,
                                         _i32, _P, _P, C.c_uint64, C.c_uint32,
                                         _i64, _P, _P, _P]),

@@ -787,6 +787,20 @@ bsg_status bsg_set_omega(bsg_ctx *ctx, int32_t chain, const double *in) {
   return BSG_OK;
 }
 
+bsg_status bsg_set_beta_wm(bsg_ctx *ctx, int32_t chain, float beta_wm) {
+  if (!valid_chain(ctx, chain) || !std::isfinite(beta_wm)) return BSG_ERR_INVALID;
+  Chain &c = ctx->ch[chain];
+  c.dev.beta_wm = beta_wm;
+  c.desc.beta_wm = beta_wm;
+  if (ctx->plan_valid) {  // graphs read the descriptor from device memory
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpyAsync(&ctx->d_ch[chain].beta_wm, &c.dev.beta_wm, sizeof(float),
+                       cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  return BSG_OK;
+}
+
 bsg_status bsg_get_colmeans(bsg_ctx *ctx, int32_t chain, float *out) {
   if (!valid_chain(ctx, chain) || !out) return BSG_ERR_INVALID;
   const Chain &c = ctx->ch[chain];
@@ -901,6 +915,131 @@ bsg_status bsg_reset_accumulators(bsg_ctx *ctx, int32_t chain) {
   CK(cudaMemset(c.dev.acc_sq, 0, sizeof(double) * n));
   if (d.S) CK(cudaMemset(c.dev.prb_sum, 0, sizeof(double) * (size_t)d.S * d.V));
   CK(cudaMemset(c.dev.nkept, 0, sizeof(long long)));
+  return BSG_OK;
+}
+
+namespace {
+struct CkptHeader {
+  uint64_t magic;
+  int32_t version, P, Vp, V, S, df_offset, burnin, thin;
+  uint32_t key0, key1, chain_id;
+  float beta_wm;
+};
+constexpr uint64_t kCkptMagic = 0x4253474C4D4D4B31ull;  // "BSGLMMK1"
+
+size_t ckpt_bytes(const Dataset &d) {
+  return sizeof(CkptHeader) + sizeof(float) * (size_t)d.P * d.Vp +
+         sizeof(double) * (size_t)d.P * d.P + sizeof(ChainCounters) +
+         sizeof(double) * ((size_t)2 * d.P * d.V + (size_t)d.S * d.V);
+}
+}  // namespace
+
+int64_t bsg_checkpoint_size(const bsg_ctx *ctx, int32_t chain) {
+  if (!valid_chain(ctx, chain)) return -1;
+  return (int64_t)ckpt_bytes(ctx->ds[ctx->ch[chain].dataset]);
+}
+
+bsg_status bsg_checkpoint(bsg_ctx *ctx, int32_t chain, void *buf, int64_t size) {
+  if (!valid_chain(ctx, chain) || !buf) return BSG_ERR_INVALID;
+  const Chain &c = ctx->ch[chain];
+  const Dataset &d = ctx->ds[c.dataset];
+  if (size < (int64_t)ckpt_bytes(d)) return fail(ctx, BSG_ERR_INVALID, "buffer too small");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  char *p = static_cast<char *>(buf);
+  CkptHeader h{kCkptMagic, 1, d.P, d.Vp, d.V, d.S, c.dev.df_offset, c.dev.burnin,
+               c.dev.thin, c.dev.key0, c.dev.key1, c.dev.chain_id, c.dev.beta_wm};
+  std::memcpy(p, &h, sizeof(h));
+  p += sizeof(h);
+  auto get = [&](const void *src, size_t n) -> cudaError_t {
+    cudaError_t e = cudaMemcpy(p, src, n, cudaMemcpyDeviceToHost);
+    p += n;
+    return e;
+  };
+  CK(get(c.dev.beta, sizeof(float) * (size_t)d.P * d.Vp));
+  CK(get(c.dev.omega_d, sizeof(double) * (size_t)d.P * d.P));
+  CK(get(counters_of(c), sizeof(ChainCounters)));
+  CK(get(c.dev.acc_sum, sizeof(double) * (size_t)d.P * d.V));
+  CK(get(c.dev.acc_sq, sizeof(double) * (size_t)d.P * d.V));
+  if (d.S) CK(get(c.dev.prb_sum, sizeof(double) * (size_t)d.S * d.V));
+  return BSG_OK;
+}
+
+bsg_status bsg_restore(bsg_ctx *ctx, int32_t chain, const void *buf, int64_t size) {
+  if (!valid_chain(ctx, chain) || !buf) return BSG_ERR_INVALID;
+  Chain &c = ctx->ch[chain];
+  const Dataset &d = ctx->ds[c.dataset];
+  CkptHeader h;
+  if (size < (int64_t)sizeof(h)) return fail(ctx, BSG_ERR_INVALID, "not a checkpoint");
+  std::memcpy(&h, buf, sizeof(h));
+  if (h.magic != kCkptMagic || h.version != 1)
+    return fail(ctx, BSG_ERR_INVALID, "not a checkpoint");
+  if (h.P != d.P || h.Vp != d.Vp || h.V != d.V || h.S != d.S ||
+      size < (int64_t)ckpt_bytes(d))
+    return fail(ctx, BSG_ERR_INVALID, "checkpoint is for a study of another shape");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const char *p = static_cast<const char *>(buf) + sizeof(h);
+  auto put = [&](void *dst, size_t n) -> cudaError_t {
+    cudaError_t e = cudaMemcpy(dst, p, n, cudaMemcpyHostToDevice);
+    p += n;
+    return e;
+  };
+  CK(put(c.dev.beta, sizeof(float) * (size_t)d.P * d.Vp));
+  std::vector<double> om((size_t)d.P * d.P);
+  std::memcpy(om.data(), p, sizeof(double) * om.size());
+  CK(put(c.dev.omega_d, sizeof(double) * om.size()));
+  std::vector<float> omf(om.begin(), om.end());
+  CK(cudaMemcpy(c.dev.omega_f, omf.data(), sizeof(float) * omf.size(),
+                cudaMemcpyHostToDevice));
+  CK(put(counters_of(c), sizeof(ChainCounters)));
+  CK(put(c.dev.acc_sum, sizeof(double) * (size_t)d.P * d.V));
+  CK(put(c.dev.acc_sq, sizeof(double) * (size_t)d.P * d.V));
+  if (d.S) CK(put(c.dev.prb_sum, sizeof(double) * (size_t)d.S * d.V));
+  c.dev.df_offset = h.df_offset;
+  c.dev.burnin = h.burnin;
+  c.dev.thin = h.thin;
+  c.dev.key0 = h.key0;
+  c.dev.key1 = h.key1;
+  c.dev.chain_id = h.chain_id;
+  c.dev.beta_wm = h.beta_wm;
+  ctx->plan_valid = false;  // descriptors changed
+  return BSG_OK;
+}
+
+bsg_status bsg_autotune(bsg_ctx *ctx, int32_t sweeps, int32_t *best_lpv,
+                        int32_t *best_threads) {
+  if (!ctx || sweeps < 1) return BSG_ERR_INVALID;
+  if (ctx->ch.empty()) return fail(ctx, BSG_ERR_STATE, "no chain");
+  std::vector<std::vector<char>> saved(ctx->ch.size());
+  for (size_t i = 0; i < ctx->ch.size(); ++i) {
+    saved[i].resize(ckpt_bytes(ctx->ds[ctx->ch[i].dataset]));
+    bsg_status s = bsg_checkpoint(ctx, (int32_t)i, saved[i].data(), (int64_t)saved[i].size());
+    if (s) return s;
+  }
+  const int lpvs[] = {1, 2, 4, 8}, thrs[] = {64, 128, 256};
+  double best = 1e300;
+  int bl = ctx->lpv, bt = ctx->threads;
+  for (int lpv : lpvs)
+    for (int thr : thrs) {
+      if (thr / lpv < 8) continue;
+      bsg_status s = bsg_set_tuning(ctx, lpv, thr);
+      if (!s) s = bsg_run(ctx, 1);  // warm-up and graph capture
+      double ms = 0;
+      if (!s) s = bsg_run_timed(ctx, sweeps, &ms);
+      for (size_t i = 0; i < ctx->ch.size() && !s; ++i)
+        s = bsg_restore(ctx, (int32_t)i, saved[i].data(), (int64_t)saved[i].size());
+      if (s) return s;
+      if (ms < best) {
+        best = ms;
+        bl = lpv;
+        bt = thr;
+      }
+    }
+  bsg_status s = bsg_set_tuning(ctx, bl, bt);
+  if (s) return s;
+  if (best_lpv) *best_lpv = bl;
+  if (best_threads) *best_threads = bt;
   return BSG_OK;
 }
 

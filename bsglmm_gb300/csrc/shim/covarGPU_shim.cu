@@ -1,0 +1,185 @@
+// covarGPU_shim.cu -- drop-in replacement for the reference's covarGPU.cu.
+//
+// The reference's mcmc() (mcmc.cpp:311-661) drives its GPU path through
+// free functions whose prototypes it declares locally (mcmc.cpp:101-125)
+// and main.cu launches setup_kernel (main.cu:410-415).  This file defines
+// those symbols with the same C++ signatures and forwards them to
+// libbsglmm_gb300.so, reading the study from the reference's own globals
+// (NSUBS, NROW, ..., hostIdx, covar).  Link it with the reference's
+// main.cu, mcmc.cpp, read_data.cpp, randgen.cpp, cholesky.cpp and covar.cpp
+// instead of covarGPU.cu.
+//
+// Mapping onto the fused sampler:
+//   updateZGPU            records the outcome array and beta_WM: the latent
+//                         draw happens inside the coefficient update;
+//   updateSpatCoefGPU     uploads Omega from the host (as the reference's
+//                         cudaMemcpyToSymbol does, covarGPU.cu:540), runs one
+//                         sweep (latent Z + beta for both colours + the
+//                         Omega draw) and returns the column means;
+//   updateSpatCoefPrecGPU writes the Omega drawn by that sweep to the host
+//                         array (covarGPU.cu:1106-1108) and advances the
+//                         host KISS stream once;
+//   compute_prbGPU        fills the reference's devicePrb and refreshes
+//                         deviceSpatCoef, which mcmc.cpp:606-607 copy back.
+// The Wishart degrees of freedom follow the reference GPU path,
+// df = TOTVOX + 19 (covarGPU.cu:1104).
+#include <cuda_runtime.h>
+#include <curand_kernel.h>
+
+#include <climits>
+#include <cstdio>
+#include <vector>
+
+#include "../../../include/bsglmm_gb300.h"
+
+// ---- globals of the reference program (main.cu, mcmc.cpp, read_data.cpp)
+extern int NSUBS, NROW, NCOL, NDEPTH, TOTVOX, TOTVOXp, NCOVAR, NSUBTYPES;
+extern int UPDATE_WM, MODEL;
+extern float logit_factor;
+extern int *hostIdx;
+extern float *deviceSpatCoef;
+extern float *devicePrb;
+double kiss(unsigned long *);  // randgen.cpp:9-23
+
+namespace {
+
+struct ShimState {
+  bsg_ctx *ctx = nullptr;
+  int32_t ds = -1, ch = -1;
+  const unsigned char *data = nullptr;
+  float beta = 0.f;
+  bool failed = false;
+  bool warned_predict = false;
+};
+ShimState g;
+
+void report(const char *where, bsg_status s) {
+  if (s == BSG_OK) return;
+  std::fprintf(stderr, "bsglmm_gb300 shim: %s: %s (%s)\n", where,
+               bsg_status_string(s), g.ctx ? bsg_last_error(g.ctx) : "");
+  g.failed = true;
+}
+
+// Creates the context on the first coefficient update: the study comes from
+// the reference's globals, the Philox key from two draws of its KISS stream.
+bool ensure(const float *covar, const float *WM, unsigned long *seed) {
+  if (g.ctx) return true;
+  if (g.failed) return false;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  bsg_status s = bsg_create(dev, &g.ctx);
+  if (s) {
+    report("bsg_create", s);
+    return false;
+  }
+  const int PX = NROW + 2, PY = NCOL + 2;
+  std::vector<uint8_t> mask((size_t)NROW * NCOL * NDEPTH);
+  for (int k = 1; k <= NDEPTH; ++k)
+    for (int j = 1; j <= NCOL; ++j)
+      for (int i = 1; i <= NROW; ++i)
+        mask[(size_t)(i - 1) + (size_t)NROW * (j - 1) + (size_t)NROW * NCOL * (k - 1)] =
+            hostIdx[i + PX * j + PX * PY * k] >= 0;
+  bsg_dataset_desc dd{};
+  dd.nrow = NROW;
+  dd.ncol = NCOL;
+  dd.ndepth = NDEPTH;
+  dd.nsubs = NSUBS;
+  dd.ncovar = NCOVAR;
+  dd.nsubtypes = NSUBTYPES;
+  dd.mask = mask.data();
+  dd.covar = covar;
+  dd.data = g.data;
+  dd.wm = UPDATE_WM ? WM : nullptr;
+  report("bsg_add_dataset", s = bsg_add_dataset(g.ctx, &dd, &g.ds));
+  if (s) return false;
+  const uint64_t hi = (uint64_t)(kiss(seed) * 4294967296.0);
+  const uint64_t lo = (uint64_t)(kiss(seed) * 4294967296.0);
+  bsg_chain_desc cd{};
+  cd.seed = (hi << 32) ^ lo;
+  cd.df_offset = 19;        // covarGPU.cu:1104
+  cd.burnin = INT_MAX;      // mcmc.cpp accumulates on the host
+  cd.thin = 1;
+  cd.beta_wm = g.beta;
+  report("bsg_add_chain", s = bsg_add_chain(g.ctx, g.ds, &cd, &g.ch));
+  return s == BSG_OK;
+}
+
+}  // namespace
+
+// main.cu:410-415 seeds one cuRAND state per voxel slot; the sampler's
+// Philox counters need no state, so this kernel does nothing.
+__global__ void setup_kernel(curandState *, unsigned long long, const int) {}
+
+void updateZGPU(unsigned char *data, float beta, unsigned long *) {
+  g.data = data;
+  g.beta = beta;
+}
+
+void updateSpatCoefGPU(float *covar, float *, float *, float *SpatCoefPrec,
+                       float *, float *alphaMean, float *, unsigned char *,
+                       float beta, float *WM, unsigned long *seed) {
+  g.beta = beta;
+  if (!ensure(covar, WM, seed)) return;
+  const int P = NCOVAR;
+  std::vector<double> om((size_t)P * P);
+  for (int i = 0; i < P * P; ++i) om[i] = (double)SpatCoefPrec[i];
+  report("bsg_set_omega", bsg_set_omega(g.ctx, g.ch, om.data()));
+  report("bsg_set_beta_wm", bsg_set_beta_wm(g.ctx, g.ch, beta));
+  report("bsg_run", bsg_run(g.ctx, 1));
+  report("bsg_sync", bsg_sync(g.ctx));
+  std::vector<float> cm(P);
+  report("bsg_get_colmeans", bsg_get_colmeans(g.ctx, g.ch, cm.data()));
+  for (int p = 0; p < P; ++p) alphaMean[p] = cm[p] / logit_factor;
+}
+
+void updateSpatCoefPrecGPU(float *SpatCoefPrec, unsigned long *seed) {
+  if (!g.ctx) return;
+  const int P = NCOVAR;
+  std::vector<double> om((size_t)P * P);
+  report("bsg_get_omega", bsg_get_omega(g.ctx, g.ch, om.data()));
+  for (int i = 0; i < P * P; ++i) SpatCoefPrec[i] = (float)om[i];
+  kiss(seed);  // the reference's Wishart draw consumes the host stream
+}
+
+void compute_prbGPU(float beta) {
+  if (!g.ctx) return;
+  report("bsg_set_beta_wm", bsg_set_beta_wm(g.ctx, g.ch, beta));
+  std::vector<float> prb((size_t)NSUBTYPES * TOTVOX + 1);
+  std::vector<float> b((size_t)NCOVAR * TOTVOXp);
+  report("bsg_compute_prb", bsg_compute_prb(g.ctx, g.ch, prb.data()));
+  report("bsg_get_beta", bsg_get_beta(g.ctx, g.ch, b.data()));
+  if (devicePrb && NSUBTYPES)
+    cudaMemcpy(devicePrb, prb.data(), sizeof(float) * (size_t)NSUBTYPES * TOTVOX,
+               cudaMemcpyHostToDevice);
+  if (deviceSpatCoef)
+    cudaMemcpy(deviceSpatCoef, b.data(), sizeof(float) * b.size(),
+               cudaMemcpyHostToDevice);
+}
+
+// The DIC / Qhat predictive pass (covarGPU.cu:1861-1957) is not part of the
+// sampler: it contributes 0 to ED and leaves Qhat unchanged.
+double compute_predictGPU(float, unsigned char *, unsigned char *, float *,
+                          float *, double **, int) {
+  if (!g.warned_predict) {
+    std::fprintf(stderr, "bsglmm_gb300 shim: compute_predictGPU (DIC/Qhat) is "
+                         "not provided; DIC.dat and Qhat*.dat are not computed\n");
+    g.warned_predict = true;
+  }
+  return 0.0;
+}
+
+// Paths the reference never takes with its shipped settings (probit
+// MODEL = 1, NCOV_FIX = 0, WM argument 0): defined so the program links,
+// they report that they are unsupported.
+void updateBetaGPU(float *, float *, float *, float *, float *, float, float,
+                   float *, float *, unsigned long *) {
+  std::fprintf(stderr, "bsglmm_gb300 shim: the WM coefficient update "
+                       "(updateBetaGPU) is not supported; beta_WM stays fixed\n");
+}
+void updatePhiGPU(float, float *) {
+  std::fprintf(stderr, "bsglmm_gb300 shim: MODEL != 1 is not supported\n");
+}
+void updatefixMeanGPU(float *, float, float *, float *, float *, float,
+                      unsigned long *) {
+  std::fprintf(stderr, "bsglmm_gb300 shim: NCOV_FIX > 0 is not supported\n");
+}

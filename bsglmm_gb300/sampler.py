@@ -178,6 +178,10 @@ class Sampler:
         a = np.ascontiguousarray(omega, dtype=np.float64).reshape(P, P)
         self._check(self._L.bsg_set_omega(self._h, chain, _ptr(a)), "bsg_set_omega")
 
+    def set_beta_wm(self, chain: int, beta_wm: float):
+        self._check(self._L.bsg_set_beta_wm(self._h, chain, float(beta_wm)),
+                    "bsg_set_beta_wm")
+
     def colmeans(self, chain: int = 0) -> np.ndarray:
         out = np.zeros(self._dims(chain)["P"], np.float32)
         self._check(self._L.bsg_get_colmeans(self._h, chain, _ptr(out)),
@@ -226,6 +230,22 @@ class Sampler:
     def reset_accumulators(self, chain: int = 0):
         self._check(self._L.bsg_reset_accumulators(self._h, chain),
                     "bsg_reset_accumulators")
+
+    def checkpoint(self, chain: int = 0) -> bytes:
+        n = int(self._L.bsg_checkpoint_size(self._h, chain))
+        buf = np.zeros(n, np.uint8)
+        self._check(self._L.bsg_checkpoint(self._h, chain, _ptr(buf), n), "bsg_checkpoint")
+        return buf.tobytes()
+
+    def restore(self, chain: int, state: bytes):
+        buf = np.frombuffer(state, np.uint8).copy()
+        self._check(self._L.bsg_restore(self._h, chain, _ptr(buf), buf.size), "bsg_restore")
+
+    def autotune(self, sweeps: int = 5):
+        a, b = C.c_int32(), C.c_int32()
+        self._check(self._L.bsg_autotune(self._h, sweeps, C.byref(a), C.byref(b)),
+                    "bsg_autotune")
+        return a.value, b.value
 
     def sweep_supplied(self, chain: int, ubits, normals, chi2, wnorm,
                        form: int = 0):

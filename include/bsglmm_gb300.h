@@ -123,6 +123,9 @@ bsg_status bsg_get_beta(bsg_ctx *ctx, int32_t chain, float *spatcoef);
 bsg_status bsg_set_beta(bsg_ctx *ctx, int32_t chain, const float *spatcoef);
 bsg_status bsg_get_omega(bsg_ctx *ctx, int32_t chain, double *omega);
 bsg_status bsg_set_omega(bsg_ctx *ctx, int32_t chain, const double *omega);
+/* Sets the fixed white-matter coefficient beta_WM of a chain (the value the
+ * reference's updateBetaGPU draws, covarGPU.cu:686-724). */
+bsg_status bsg_set_beta_wm(bsg_ctx *ctx, int32_t chain, float beta_wm);
 /* Column means of the last sweep (covarGPU.cu:563-583). */
 bsg_status bsg_get_colmeans(bsg_ctx *ctx, int32_t chain, float *means);
 bsg_status bsg_get_sweep(bsg_ctx *ctx, int32_t chain, int64_t *sweep,
@@ -141,6 +144,22 @@ bsg_status bsg_get_maps(bsg_ctx *ctx, int32_t chain, double *spatcoef,
                         double *spatcoef_var, double *standcoef, double *prb);
 /* Clears the posterior accumulators and the kept-sweep count. */
 bsg_status bsg_reset_accumulators(bsg_ctx *ctx, int32_t chain);
+
+/* ------------------------------------------------- checkpoint / tuning -- */
+/* A chain's complete state: coefficients, Omega, sweep counters, posterior
+ * sums, Philox key and chain id.  Counter-based variates make a restored
+ * chain continue bit-exactly, in this or another context (same study
+ * shape).  The reference's save_iter/restart_iter (mcmc.cpp:1265-1336) are
+ * never called; this replaces them. */
+int64_t bsg_checkpoint_size(const bsg_ctx *ctx, int32_t chain);
+bsg_status bsg_checkpoint(bsg_ctx *ctx, int32_t chain, void *buf, int64_t size);
+bsg_status bsg_restore(bsg_ctx *ctx, int32_t chain, const void *buf,
+                       int64_t size);
+/* Times each supported tile shape (lanes per voxel x threads per block) on
+ * the context's chains for `sweeps` sweeps, keeps the fastest and puts every
+ * chain back to its state before the call. */
+bsg_status bsg_autotune(bsg_ctx *ctx, int32_t sweeps, int32_t *lanes_per_voxel,
+                        int32_t *block_threads);
 
 /* ---------------------------------------------------- parity interface -- */
 /* One sweep of one chain driven by supplied variates instead of Philox:

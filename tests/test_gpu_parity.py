@@ -264,3 +264,51 @@ def test_non_spd_precision_reported(bsg):
         with pytest.raises(bsg.BsgError) as e:
             s.run(1)
         assert e.value.status == 3  # BSG_ERR_NOT_SPD
+
+
+# ------------------------------------------------- checkpoint / autotune --
+def test_checkpoint_resume_is_bit_exact(bsg):
+    st = _study(81, shape=(10, 9, 11), N=70, P=4, S=2)
+    with bsg.Sampler() as s:
+        ds = s.add_dataset(st.mask, st.covar, st.data, 2)
+        ch = s.add_chain(ds, seed=4242, burnin=3)
+        s.run(6)
+        ck = s.checkpoint(ch)
+        s.run(5)
+        ref = (s.beta(ch), s.omega(ch), s.posterior(ch))
+    with bsg.Sampler() as s:  # another context, the chain at another index
+        ds0 = s.add_dataset(st.mask, st.covar, st.data, 2)
+        s.add_chain(ds0, seed=1)
+        ch = s.add_chain(ds0, seed=999)
+        s.restore(ch, ck)
+        s.run(5)
+        assert np.array_equal(s.beta(ch), ref[0])
+        assert np.array_equal(s.omega(ch), ref[1])
+        m, v, p, nk = s.posterior(ch)
+        assert nk == ref[2][3] and np.array_equal(m, ref[2][0])
+        assert np.array_equal(p, ref[2][2])
+
+
+def test_restore_rejects_other_shapes(bsg):
+    a = _study(82, shape=(8, 8, 8), N=40, P=3, S=1)
+    b = _study(83, shape=(9, 8, 8), N=40, P=3, S=1)
+    with bsg.Sampler() as s:
+        ca = s.add_chain(s.add_dataset(a.mask, a.covar, a.data, 1), seed=1)
+        cb = s.add_chain(s.add_dataset(b.mask, b.covar, b.data, 1), seed=1)
+        ck = s.checkpoint(ca)
+        with pytest.raises(bsg.BsgError):
+            s.restore(cb, ck)
+        with pytest.raises(bsg.BsgError):
+            s.restore(ca, b"not a checkpoint" * 8)
+
+
+def test_autotune_restores_state(bsg):
+    st = _study(84, shape=(12, 12, 12), N=200, P=5, S=1)
+    with bsg.Sampler() as s:
+        ch = s.add_chain(s.add_dataset(st.mask, st.covar, st.data, 1), seed=77)
+        s.run(2)
+        b0, o0, sw0 = s.beta(ch), s.omega(ch), s.sweep_count(ch)
+        lpv, thr = s.autotune(2)
+        assert (lpv, thr) == s.tuning()
+        assert np.array_equal(s.beta(ch), b0) and np.array_equal(s.omega(ch), o0)
+        assert s.sweep_count(ch) == sw0

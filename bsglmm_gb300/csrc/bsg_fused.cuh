@@ -42,7 +42,8 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
                         const BlockMap *__restrict__ map, int colour,
                         Supplied sup) {
   constexpr int NT = P * (P + 1) / 2;
-  __shared__ float Xs[P][kChunkPad];
+  constexpr int PP = P <= 4 ? 4 : 8;  // design row padded to float4s
+  __shared__ __align__(16) float Xs[kChunkPad][PP];
   __shared__ float Om[P * P], Xtx[P * P];
 
   const BlockMap bm = map[blockIdx.x];
@@ -88,7 +89,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
     __syncthreads();
     for (int t = tid; t < P * kChunk; t += blockDim.x) {
       const int p = t / kChunk, ii = t - p * kChunk;
-      Xs[p][ii + (ii >> 5)] = ii < cn ? d.covar[(size_t)p * N + i0 + ii] : 0.f;
+      Xs[ii + (ii >> 5)][p] = ii < cn ? d.covar[(size_t)p * N + i0 + ii] : 0.f;
     }
     __syncthreads();
     if (active) {
@@ -97,19 +98,32 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
       // Z - bwm = x'beta + (Y ? t : -t); acc += x (Z - bwm).
       auto subject = [&](int col, uint32_t ymask, uint32_t kk, uint32_t isub) {
         float x[P];
+        const float4 v0 = *reinterpret_cast<const float4 *>(&Xs[col][0]);
+        x[0] = v0.x;
+        if (P > 1) x[1] = v0.y;
+        if (P > 2) x[2] = v0.z;
+        if (P > 3) x[3] = v0.w;
+        if (P > 4) {
+          const float4 v1 = *reinterpret_cast<const float4 *>(&Xs[col][4]);
+          x[4] = v1.x;
+          if (P > 5) x[5] = v1.y;
+          if (P > 6) x[6] = v1.z;
+          if (P > 7) x[7] = v1.w;
+        }
         float m0 = 0.f;
 #pragma unroll
-        for (int p = 0; p < P; ++p) {
-          x[p] = Xs[p][col];
-          m0 = fmaf(beta[p], x[p], m0);
-        }
+        for (int p = 0; p < P; ++p) m0 = fmaf(beta[p], x[p], m0);
         const float a = __uint_as_float(__float_as_uint(m0 + bwm) ^ ymask);
         float t;
-        if (SUPP || a <= kATail) {
+        if (SUPP) {
           t = tn_lower_inv(a, kk);
         } else {
-          t = tn_lower_tail(a, isub, (uint32_t)v, sweep, cid | kTagZTail,
-                            ch.key0, ch.key1, &ok);
+          t = tn_lower_inv(fminf(a, kATail), kk);
+          // beyond 5 sigma: bounded rejection, entered by a warp only when
+          // one of its lanes needs it
+          if (__any_sync(__activemask(), a > kATail) && a > kATail)
+            t = tn_lower_tail(a, isub, (uint32_t)v, sweep, cid | kTagZTail,
+                              ch.key0, ch.key1, &ok);
         }
         const float zr = m0 + __uint_as_float(__float_as_uint(t) ^ ymask ^ 0x80000000u);
 #pragma unroll

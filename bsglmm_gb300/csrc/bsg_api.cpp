@@ -70,6 +70,7 @@ struct bsg_ctx {
   size_t d_ds_cap = 0, d_ch_cap = 0;
   bool plan_valid = false;
   std::vector<Group> groups;
+  int *any_status = nullptr;  // device word: OR of every chain's error bits
   int lpv = 1, threads = 256;
 #ifdef BSG_NO_PDL
   bool pdl = false;
@@ -565,6 +566,12 @@ bsg_status bsg_add_chain(bsg_ctx *ctx, int32_t dataset_id,
   cv.nkept = &cnt->nkept;
   cv.done = cnt->done;
   cv.status = &cnt->status;
+  if (!ctx->any_status) {
+    ctx->any_status = (int *)dalloc(ctx, sizeof(int), &e);
+    CK(e);
+    CK(cudaMemset(ctx->any_status, 0, sizeof(int)));
+  }
+  cv.any_status = ctx->any_status;
   ctx->ch.push_back(c);
   *chain_id = (int32_t)ctx->ch.size() - 1;
   ctx->plan_valid = false;
@@ -616,13 +623,15 @@ bsg_status bsg_sync(bsg_ctx *ctx) {
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   int bits = 0;
-  for (auto &c : ctx->ch) {
-    int b = 0;
-    CK(cudaMemcpy(&b, c.dev.status, sizeof(int), cudaMemcpyDeviceToHost));
-    bits |= b;
-  }
+  if (ctx->any_status)
+    CK(cudaMemcpy(&bits, ctx->any_status, sizeof(int), cudaMemcpyDeviceToHost));
   if (bits) {
     ctx->err = "sampler:" + status_text(bits);
+    for (size_t i = 0; i < ctx->ch.size(); ++i) {
+      int b = 0;
+      CK(cudaMemcpy(&b, ctx->ch[i].dev.status, sizeof(int), cudaMemcpyDeviceToHost));
+      if (b) ctx->err += " (chain " + std::to_string(i) + ")";
+    }
     return status_from_bits(bits);
   }
   return BSG_OK;

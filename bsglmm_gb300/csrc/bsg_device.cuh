@@ -91,15 +91,24 @@ __device__ __forceinline__ float normal_of(uint32_t k) {
 }
 
 // N(0,1) truncated to (a, +inf) by inversion of u(k):
-//   t = Phi^-1(Phi(a) + u Q(a)),  evaluated as -Phi^-1(Q(a) (1-u)) once the
-// argument passes 1/2, so both tails keep relative precision.
+//   t = Phi^-1(Phi(a) + u Q(a)).  With T = Q(|a|):
+//   a >= 0:  the argument is >= 1/2, so t = -Phi^-1(T (1-u));
+//   a <  0:  the argument is u + T (1-u); below 1/2 t = Phi^-1 of it, else
+//            t = -Phi^-1((1-T)(1-u)).
+// Both tails keep relative precision; 1 - u = u(~k) comes from the integer.
+// CLAMP guards the argument against underflow when a is unbounded (the
+// supplied-variate path); the sampler clamps a at the 5-sigma switch.
+template <bool CLAMP = false>
 __device__ __forceinline__ float tn_lower_inv(float a, uint32_t k) {
-  const float T = phi_tail(fabsf(a));  // mass beyond |a|
-  const float Pa = a < 0.f ? T : 1.f - T;
-  const float Qa = a < 0.f ? 1.f - T : T;
-  const float pl = fmaf(u_of(k), Qa, Pa);
-  const bool lo = pl < 0.5f;
-  const float t = ndtri_lower(lo ? pl : Qa * u_of(~k));
+  const float T = phi_tail(fabsf(a));
+  const float uc = u_of(~k);
+  const float tuc = T * uc;
+  const float q1 = fmaf(T, uc, u_of(k));
+  const bool neg = a < 0.f;
+  const bool lo = neg && q1 < 0.5f;
+  float arg = lo ? q1 : (neg ? uc - tuc : tuc);
+  if (CLAMP) arg = fmaxf(arg, 1.17549435e-38f);
+  const float t = ndtri_lower(arg);
   return lo ? t : -t;
 }
 

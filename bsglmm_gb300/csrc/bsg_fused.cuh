@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
         const float a = __uint_as_float(__float_as_uint(m0 + bwm) ^ ymask);
         float t;
         if (SUPP) {
-          t = tn_lower_inv(a, kk);
+          t = tn_lower_inv<true>(a, kk);
         } else {
           t = tn_lower_inv(fminf(a, kATail), kk);
           // beyond 5 sigma: bounded rejection, entered by a warp only when
@@ -339,7 +339,10 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
 #pragma unroll
     for (int p = 0; p < P; ++p) bnew[p] = 0.f;  // no column-sum share
   }
-  if (err) atomicOr(ch.status, err);
+  if (err) {
+    atomicOr(ch.status, err);
+    atomicOr(ch.any_status, err);
+  }
 
   // ---- block partials: column sums (both colours) and pairs (colour 1) --
   __shared__ double red[kMaxThreads / 32][kPostVals];

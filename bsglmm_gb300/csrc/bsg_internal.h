@@ -72,7 +72,8 @@ struct ChainDev {
   long long *sweep;        // [2] sweeps completed by the colour-c kernel;
                            // sweep[1] is the chain's completed-sweep count
   long long *nkept;        // kept sweeps accumulated
-  int *status;             // sticky error bits
+  int *status;             // sticky error bits of this chain
+  int *any_status;         // the context's OR of every chain's bits
 };
 
 // Parity mode: variates supplied by the caller instead of Philox.

@@ -68,23 +68,21 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
   return y;
 }
 
-// Q(x) for x >= 0.  x*x is split into hi + lo so the exponent keeps full
-// precision up to the 5-sigma switch of the latent sampler:
-// exp(-x^2/2) = 2^(-hi log2(e)/2) (1 - lo/2).
+// Q(x) for x >= 0.  The rounding of x*x costs at most 7.5e-7 relative at
+// the 5-sigma switch of the latent sampler (the only range where Q's
+// relative precision matters).
 __device__ __forceinline__ float phi_tail(float x) {
-  const float hi = x * x;
-  const float lo = fmaf(x, x, -hi);
-  float e = ex2_approx(hi * -0.72134752044448170f);
-  e = fmaf(e * lo, -0.5f, e);
+  const float e = ex2_approx(x * (x * -0.72134752044448170f));
   const float n = fmaf(fmaf(fmaf(kMillsN3, x, kMillsN2), x, kMillsN1), x, kMillsN0);
   const float d = fmaf(fmaf(fmaf(fmaf(kMillsD4, x, kMillsD3), x, kMillsD2), x,
                             kMillsD1), x, 1.0f);
   return e * n * rcp_approx(d);
 }
 
-// Phi^-1(p), 0 < p <= 1/2 (p below the smallest normal float is clamped).
+// Phi^-1(p), 0 < p <= 1/2; p must be a normal float (callers clamp where
+// it could underflow).
 __device__ __forceinline__ float ndtri_lower(float p) {
-  const float l = -lg2_approx(fmaxf(p, 1.17549435e-38f));  // >= 1
+  const float l = -lg2_approx(p);  // >= 1
   const float rho = l * rsqrt_approx(l);
   const float n = fmaf(fmaf(fmaf(fmaf(fmaf(kNdtN5, rho, kNdtN4), rho, kNdtN3),
                                  rho, kNdtN2), rho, kNdtN1), rho, kNdtN0);

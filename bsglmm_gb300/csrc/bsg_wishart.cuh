@@ -155,7 +155,10 @@ static __device__ void wishart_warp(const ChainDev &ch, const DatasetDev &d,
   if (lane < P) ch.colmean[lane] = (float)(tot[kMaxPairs + lane] / (double)d.V);
   err = __reduce_or_sync(0xffffffffu, err);
   if (lane == 0) {
-    if (err) atomicOr(ch.status, err);
+    if (err) {
+      atomicOr(ch.status, err);
+      atomicOr(ch.any_status, err);
+    }
     ch.sweep[1] = sweep + 1;
     if (kept) *ch.nkept = nk + 1;
     ch.done[1] = 0u;

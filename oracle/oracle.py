@@ -359,7 +359,22 @@ class RefKiss(_Ref):
         L.ref_snorm_many.argtypes = [_i, _P]
         L.ref_rgamma_many.argtypes = [_d, _d, _i, _P]
         L.ref_cpu_sweep.argtypes = [_P, _P, _P, _P, _P, _P]
+        L.ref_kiss_many.argtypes = [_i, _P, _P]
+        L.ref_write_nifti.argtypes = [_i, _i, _i, C.c_char_p, _P]
         L.ref_kiss_seed(*seed)
+
+    def write_nifti(self, path, data_zyx):
+        """The reference's .nii writer on a [Z][Y][X] volume."""
+        d = np.ascontiguousarray(data_zyx, dtype=np.float64)
+        Z, Y, X = d.shape
+        return self._L.ref_write_nifti(X, Y, Z, str(path).encode(), _p(d))
+
+    def kiss(self, n):
+        """n raw KISS draws and the generator state after them."""
+        out = np.zeros(n)
+        state = np.zeros(3, np.uint64)
+        self._L.ref_kiss_many(n, _p(out), _p(state))
+        return out, [int(x) for x in state]
 
     def truncnorm(self, mu, lo, hi, n):
         out = np.zeros(n)

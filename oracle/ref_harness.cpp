@@ -97,6 +97,7 @@ double rgamma(double alpha, double beta, unsigned long *) {
 }
 #else
 double kiss(unsigned long *);
+int write_nifti_file(int, int, int, int, char *, char *, double *);  /* nifti1_read_write.cpp */
 double sgamma(double, unsigned long *);
 #endif
 
@@ -240,6 +241,17 @@ void ref_kiss_seed(uint64_t a, uint64_t b, uint64_t c) {
   g_seed[0] = (unsigned long)a;
   g_seed[1] = (unsigned long)b;
   g_seed[2] = (unsigned long)c;
+}
+/* The reference's single-file NIfTI-1 writer (nifti1_read_write.cpp:198-322)
+ * on a volume of FLOAT64 values, x fastest. */
+int ref_write_nifti(int nrow, int ncol, int ndepth, const char *path, double *data) {
+  return write_nifti_file(nrow, ncol, ndepth, 1, (char *)path, (char *)path, data);
+}
+/* n raw draws of the reference's KISS generator (randgen.cpp:9-23), then
+ * its state, as the program writes it back to seed.dat (main.cu:430-432). */
+void ref_kiss_many(int n, double *out, uint64_t *state) {
+  for (int i = 0; i < n; ++i) out[i] = kiss(g_seed);
+  for (int i = 0; i < 3; ++i) state[i] = (uint64_t)g_seed[i];
 }
 /* The reference's own samplers on its KISS stream (randgen.cpp). */
 void ref_truncnorm_many(double mu, double lo, double hi, int n, double *out) {

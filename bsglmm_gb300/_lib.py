@@ -53,6 +53,11 @@ SIGNATURES = {
     "bsg_get_posterior": (_i32, [_P, _i32, _P, _P, _P, C.POINTER(_i64)]),
     "bsg_get_maps": (_i32, [_P, _i32, _P, _P, _P, _P]),
     "bsg_reset_accumulators": (_i32, [_P, _i32]),
+    "bsg_set_predictive": (_i32, [_P, _i32, _i32]),
+    "bsg_predict": (_i32, [_P, _i32, _P]),
+    "bsg_get_predictive": (_i32, [_P, _i32, _P, C.POINTER(C.c_double),
+                                  C.POINTER(C.c_int64)]),
+    "bsg_get_dic": (_i32, [_P, _i32, _P]),
     "bsg_sweep_supplied": (_i32, [_P, _i32, _P, _P, _P, _P, _i32]),
     "bsg_fp32_peak": (_i32, [_i32, C.POINTER(C.c_double)]),
     "bsg_checkpoint_size": (_i64, [_P, _i32]),

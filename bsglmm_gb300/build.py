@@ -30,6 +30,7 @@ SOURCES = [
     "bsg_kernels.cu",
     "bsg_peak.cu",
     "bsg_noalloc.cu",
+    "bsg_predict.cu",
     "bsg_api.cpp",
 ]
 HEADERS = ["bsg_device.cuh", "bsg_fused.cuh", "bsg_internal.h", "bsg_math.cuh"]

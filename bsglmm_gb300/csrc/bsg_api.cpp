@@ -38,12 +38,25 @@ struct Chain {
   bsg_chain_desc desc{};
   ChainDev dev{};
   size_t cap0 = 0, cap1 = 0;  // partial rows allocated per colour
+  bool pred_on = false;        // predictive pass after every kept sweep
 };
 
 struct Group {
   int P = 0;
   std::vector<BlockMap> map[2];
   BlockMap *d_map[2] = {nullptr, nullptr};
+  // predictive pass of the group's chains that have it on: {chain, tile}
+  // blocks, {chain, subject block} finishing blocks, subject chunks
+  std::vector<BlockMap> pmap, fmap;
+  BlockMap *d_pmap = nullptr, *d_fmap = nullptr;
+  int pchunks = 0;
+};
+
+// Small per-chain counters of the predictive pass.
+struct PredCounters {
+  long long npred;
+  unsigned int done;
+  int pad;
 };
 
 // Small per-chain counters kept together on the device.
@@ -262,8 +275,11 @@ bsg_status build_plan(bsg_ctx *ctx) {
                 cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_ch, hch.data(), sizeof(ChainDev) * hch.size(),
                 cudaMemcpyHostToDevice));
-  for (auto &g : ctx->groups)
+  for (auto &g : ctx->groups) {
     for (int c = 0; c < 2; ++c) dfree(ctx, g.d_map[c]);
+    dfree(ctx, g.d_pmap);
+    dfree(ctx, g.d_fmap);
+  }
   ctx->groups.clear();
   for (size_t ci = 0; ci < ctx->ch.size(); ++ci) {
     const Dataset &d = ctx->ds[ctx->ch[ci].dataset];
@@ -276,12 +292,25 @@ bsg_status build_plan(bsg_ctx *ctx) {
       g->P = d.P;
     }
     for (int c = 0; c < 2; ++c) map_chain(g->map[c], (int)ci, (int)d.vox[c].size(), vpb, c);
+    if (ctx->ch[ci].pred_on) {
+      const ChainDev &cv = ctx->ch[ci].dev;
+      for (int t = 0; t < cv.pred_tiles; ++t) g->pmap.push_back({(int32_t)ci, (int32_t)t});
+      for (int b = 0; b * kPredWarps < d.N; ++b) g->fmap.push_back({(int32_t)ci, (int32_t)b});
+      g->pchunks = std::max(g->pchunks, (d.N + kPredThreads - 1) / kPredThreads);
+    }
   }
-  for (auto &g : ctx->groups)
+  for (auto &g : ctx->groups) {
     for (int c = 0; c < 2; ++c) {
       g.d_map[c] = upload(ctx, g.map[c].data(), g.map[c].size(), &e);
       CK(e);
     }
+    if (!g.pmap.empty()) {
+      g.d_pmap = upload(ctx, g.pmap.data(), g.pmap.size(), &e);
+      CK(e);
+      g.d_fmap = upload(ctx, g.fmap.data(), g.fmap.size(), &e);
+      CK(e);
+    }
+  }
   while (ctx->side.size() < ctx->groups.size()) {
     cudaStream_t s;
     cudaEvent_t ev;
@@ -297,29 +326,37 @@ bsg_status build_plan(bsg_ctx *ctx) {
 // Enqueues one sweep of every chain: per P group the two colour kernels
 // (groups on parallel branches when there are several); the colour-1
 // kernel also reduces the Omega pairs and draws Omega.
-cudaError_t enqueue_sweep(bsg_ctx *ctx, cudaStream_t st) {
+cudaError_t enqueue_group(bsg_ctx *ctx, const Group &g, cudaStream_t st) {
   const Supplied sup{};
   cudaError_t e;
+  for (int c = 0; c < 2; ++c) {
+    e = launch_fused(g.P, ctx->lpv, ctx->threads, false, ctx->d_ds, ctx->d_ch,
+                     g.d_map[c], (int)g.map[c].size(), c, sup, st, ctx->pdl);
+    if (e != cudaSuccess) return e;
+  }
+  if (!g.pmap.empty()) {
+    // DIC / Qhat pass; its blocks return at once unless the sweep is kept
+    e = launch_predict(g.P, ctx->d_ds, ctx->d_ch, g.d_pmap, (int)g.pmap.size(),
+                       g.pchunks, 0, kPredKept, st, ctx->pdl);
+    if (e != cudaSuccess) return e;
+    e = launch_predict_finish(ctx->d_ds, ctx->d_ch, g.d_fmap, (int)g.fmap.size(), 0,
+                              kPredKept, st, ctx->pdl);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t enqueue_sweep(bsg_ctx *ctx, cudaStream_t st) {
+  cudaError_t e;
   if (ctx->groups.size() == 1) {
-    const Group &g = ctx->groups[0];
-    for (int c = 0; c < 2; ++c) {
-      e = launch_fused(g.P, ctx->lpv, ctx->threads, false, ctx->d_ds,
-                       ctx->d_ch, g.d_map[c], (int)g.map[c].size(), c, sup, st,
-                       ctx->pdl);
-      if (e != cudaSuccess) return e;
-    }
+    if ((e = enqueue_group(ctx, ctx->groups[0], st)) != cudaSuccess) return e;
   } else {
     if ((e = cudaEventRecord(ctx->fork, st)) != cudaSuccess) return e;
     for (size_t gi = 0; gi < ctx->groups.size(); ++gi) {
       const Group &g = ctx->groups[gi];
       cudaStream_t s = ctx->side[gi];
       if ((e = cudaStreamWaitEvent(s, ctx->fork, 0)) != cudaSuccess) return e;
-      for (int c = 0; c < 2; ++c) {
-        e = launch_fused(g.P, ctx->lpv, ctx->threads, false, ctx->d_ds,
-                         ctx->d_ch, g.d_map[c], (int)g.map[c].size(), c, sup, s,
-                         ctx->pdl);
-        if (e != cudaSuccess) return e;
-      }
+      if ((e = enqueue_group(ctx, g, s)) != cudaSuccess) return e;
       if ((e = cudaEventRecord(ctx->join[gi], s)) != cudaSuccess) return e;
       if ((e = cudaStreamWaitEvent(st, ctx->join[gi], 0)) != cudaSuccess) return e;
     }
@@ -360,6 +397,43 @@ bool valid_chain(const bsg_ctx *ctx, int32_t c) {
 
 ChainCounters *counters_of(const Chain &c) {
   return reinterpret_cast<ChainCounters *>(c.dev.sweep);  // first member
+}
+
+PredCounters *pred_counters_of(const Chain &c) {
+  return reinterpret_cast<PredCounters *>(c.dev.npred);  // first member
+}
+
+// Buffers of the predictive pass, allocated on first use (zeroed).
+bsg_status ensure_pred(bsg_ctx *ctx, Chain &c) {
+  if (c.dev.pred_part) return BSG_OK;
+  const Dataset &d = ctx->ds[c.dataset];
+  const int ntot = (int)(d.vox[0].size() + d.vox[1].size());
+  const int T = std::max(1, (ntot + kPredTile - 1) / kPredTile);
+  const size_t N = (size_t)d.N, G = (size_t)std::max(d.S, 1);
+  cudaError_t e;
+  ChainDev &cv = c.dev;
+  double *part = (double *)dalloc(ctx, sizeof(double) * T * N * G, &e);
+  CK(e);
+  cv.pred_subj = (double *)dalloc(ctx, sizeof(double) * N, &e);
+  CK(e);
+  cv.mpred = (double *)dalloc(ctx, sizeof(double) * N * G, &e);
+  CK(e);
+  cv.qhat = (double *)dalloc(ctx, sizeof(double) * N * G, &e);
+  CK(e);
+  cv.pred_sums = (double *)dalloc(ctx, sizeof(double) * 2, &e);
+  CK(e);
+  PredCounters *pc = (PredCounters *)dalloc(ctx, sizeof(PredCounters), &e);
+  CK(e);
+  CK(cudaMemset(cv.mpred, 0, sizeof(double) * N * G));
+  CK(cudaMemset(cv.qhat, 0, sizeof(double) * N * G));
+  CK(cudaMemset(cv.pred_sums, 0, sizeof(double) * 2));
+  CK(cudaMemset(pc, 0, sizeof(PredCounters)));
+  cv.npred = &pc->npred;
+  cv.pred_done = &pc->done;
+  cv.pred_tiles = T;
+  cv.pred_part = part;
+  ctx->plan_valid = false;  // the device copy of the chain changed
+  return BSG_OK;
 }
 
 }  // namespace
@@ -709,14 +783,13 @@ bsg_status bsg_profile(bsg_ctx *ctx, int64_t nsweeps, double *ms,
 
 int64_t bsg_launches_per_sweep(const bsg_ctx *ctx) {
   if (!ctx) return 0;
-  size_t ng = 0;
-  std::vector<int> ps;
+  std::vector<int> ps, pp;
   for (auto &c : ctx->ch) {
     const int P = ctx->ds[c.dataset].P;
     if (std::find(ps.begin(), ps.end(), P) == ps.end()) ps.push_back(P);
+    if (c.pred_on && std::find(pp.begin(), pp.end(), P) == pp.end()) pp.push_back(P);
   }
-  ng = ps.size();
-  return (int64_t)(2 * ng);
+  return (int64_t)(2 * ps.size() + 2 * pp.size());
 }
 
 void *bsg_stream(bsg_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
@@ -924,6 +997,11 @@ bsg_status bsg_reset_accumulators(bsg_ctx *ctx, int32_t chain) {
   CK(cudaMemset(c.dev.acc_sq, 0, sizeof(double) * n));
   if (d.S) CK(cudaMemset(c.dev.prb_sum, 0, sizeof(double) * (size_t)d.S * d.V));
   CK(cudaMemset(c.dev.nkept, 0, sizeof(long long)));
+  if (c.dev.pred_part) {
+    CK(cudaMemset(c.dev.qhat, 0, sizeof(double) * (size_t)d.N * std::max(d.S, 1)));
+    CK(cudaMemset(c.dev.pred_sums, 0, sizeof(double) * 2));
+    CK(cudaMemset(c.dev.npred, 0, sizeof(long long)));
+  }
   return BSG_OK;
 }
 
@@ -936,10 +1014,22 @@ struct CkptHeader {
 };
 constexpr uint64_t kCkptMagic = 0x4253474C4D4D4B31ull;  // "BSGLMMK1"
 
-size_t ckpt_bytes(const Dataset &d) {
+// Version 2 appends the predictive pass: PredCkpt and Qhat [N][max(S,1)].
+struct PredCkpt {
+  int32_t on, allocated;
+  long long npred;
+  double ed_sum;
+};
+
+size_t ckpt_bytes_v1(const Dataset &d) {
   return sizeof(CkptHeader) + sizeof(float) * (size_t)d.P * d.Vp +
          sizeof(double) * (size_t)d.P * d.P + sizeof(ChainCounters) +
          sizeof(double) * ((size_t)2 * d.P * d.V + (size_t)d.S * d.V);
+}
+
+size_t ckpt_bytes(const Dataset &d) {
+  return ckpt_bytes_v1(d) + sizeof(PredCkpt) +
+         sizeof(double) * (size_t)d.N * std::max(d.S, 1);
 }
 }  // namespace
 
@@ -956,7 +1046,7 @@ bsg_status bsg_checkpoint(bsg_ctx *ctx, int32_t chain, void *buf, int64_t size) 
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   char *p = static_cast<char *>(buf);
-  CkptHeader h{kCkptMagic, 1, d.P, d.Vp, d.V, d.S, c.dev.df_offset, c.dev.burnin,
+  CkptHeader h{kCkptMagic, 2, d.P, d.Vp, d.V, d.S, c.dev.df_offset, c.dev.burnin,
                c.dev.thin, c.dev.key0, c.dev.key1, c.dev.chain_id, c.dev.beta_wm};
   std::memcpy(p, &h, sizeof(h));
   p += sizeof(h);
@@ -971,6 +1061,18 @@ bsg_status bsg_checkpoint(bsg_ctx *ctx, int32_t chain, void *buf, int64_t size) 
   CK(get(c.dev.acc_sum, sizeof(double) * (size_t)d.P * d.V));
   CK(get(c.dev.acc_sq, sizeof(double) * (size_t)d.P * d.V));
   if (d.S) CK(get(c.dev.prb_sum, sizeof(double) * (size_t)d.S * d.V));
+  const size_t nq = (size_t)d.N * std::max(d.S, 1);
+  PredCkpt pk{c.pred_on ? 1 : 0, c.dev.pred_part ? 1 : 0, 0, 0.0};
+  if (c.dev.pred_part) {
+    CK(cudaMemcpy(&pk.npred, c.dev.npred, sizeof(long long), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&pk.ed_sum, c.dev.pred_sums, sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  std::memcpy(p, &pk, sizeof(pk));
+  p += sizeof(pk);
+  if (c.dev.pred_part)
+    CK(get(c.dev.qhat, sizeof(double) * nq));
+  else
+    std::memset(p, 0, sizeof(double) * nq);
   return BSG_OK;
 }
 
@@ -981,10 +1083,10 @@ bsg_status bsg_restore(bsg_ctx *ctx, int32_t chain, const void *buf, int64_t siz
   CkptHeader h;
   if (size < (int64_t)sizeof(h)) return fail(ctx, BSG_ERR_INVALID, "not a checkpoint");
   std::memcpy(&h, buf, sizeof(h));
-  if (h.magic != kCkptMagic || h.version != 1)
+  if (h.magic != kCkptMagic || (h.version != 1 && h.version != 2))
     return fail(ctx, BSG_ERR_INVALID, "not a checkpoint");
   if (h.P != d.P || h.Vp != d.Vp || h.V != d.V || h.S != d.S ||
-      size < (int64_t)ckpt_bytes(d))
+      size < (int64_t)(h.version == 1 ? ckpt_bytes_v1(d) : ckpt_bytes(d)))
     return fail(ctx, BSG_ERR_INVALID, "checkpoint is for a study of another shape");
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -1005,6 +1107,24 @@ bsg_status bsg_restore(bsg_ctx *ctx, int32_t chain, const void *buf, int64_t siz
   CK(put(c.dev.acc_sum, sizeof(double) * (size_t)d.P * d.V));
   CK(put(c.dev.acc_sq, sizeof(double) * (size_t)d.P * d.V));
   if (d.S) CK(put(c.dev.prb_sum, sizeof(double) * (size_t)d.S * d.V));
+  PredCkpt pk{0, 0, 0, 0.0};
+  if (h.version == 2) {
+    std::memcpy(&pk, p, sizeof(pk));
+    p += sizeof(pk);
+  }
+  if (pk.allocated || c.dev.pred_part) {
+    bsg_status ps = ensure_pred(ctx, c);
+    if (ps) return ps;
+    const size_t nq = (size_t)d.N * std::max(d.S, 1);
+    if (pk.allocated)
+      CK(put(c.dev.qhat, sizeof(double) * nq));
+    else
+      CK(cudaMemset(c.dev.qhat, 0, sizeof(double) * nq));
+    CK(cudaMemcpy(c.dev.npred, &pk.npred, sizeof(long long), cudaMemcpyHostToDevice));
+    const double sums[2] = {pk.ed_sum, 0.0};
+    CK(cudaMemcpy(c.dev.pred_sums, sums, sizeof(sums), cudaMemcpyHostToDevice));
+  }
+  c.pred_on = pk.on != 0;
   c.dev.df_offset = h.df_offset;
   c.dev.burnin = h.burnin;
   c.dev.thin = h.thin;
@@ -1097,6 +1217,101 @@ bsg_status bsg_sweep_supplied(bsg_ctx *ctx, int32_t chain, const uint32_t *ubits
                   (void *)dm1})
     dfree(ctx, p);
   return bsg_sync(ctx);
+}
+
+// ------------------------------------------------ DIC / Qhat predictive --
+bsg_status bsg_set_predictive(bsg_ctx *ctx, int32_t chain, int32_t enable) {
+  if (!valid_chain(ctx, chain)) return BSG_ERR_INVALID;
+  Chain &c = ctx->ch[chain];
+  if (ctx->ds[c.dataset].S < 1)
+    return fail(ctx, BSG_ERR_INVALID, "the predictive pass needs a group column (S >= 1)");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (enable) {
+    bsg_status s = ensure_pred(ctx, c);
+    if (s) return s;
+  }
+  if (c.pred_on != (enable != 0)) ctx->plan_valid = false;
+  c.pred_on = enable != 0;
+  return BSG_OK;
+}
+
+bsg_status bsg_predict(bsg_ctx *ctx, int32_t chain, double *mpredict) {
+  if (!valid_chain(ctx, chain) || !mpredict) return BSG_ERR_INVALID;
+  Chain &c = ctx->ch[chain];
+  const Dataset &d = ctx->ds[c.dataset];
+  if (d.S < 1)
+    return fail(ctx, BSG_ERR_INVALID, "the predictive pass needs a group column (S >= 1)");
+  CK(cudaSetDevice(ctx->device));
+  bsg_status s = ensure_pred(ctx, c);
+  if (s) return s;
+  if ((s = build_plan(ctx))) return s;
+  const int chunks = (d.N + kPredThreads - 1) / kPredThreads;
+  CK(launch_predict(d.P, ctx->d_ds, ctx->d_ch, nullptr, c.dev.pred_tiles, chunks,
+                    chain, kPredNow, ctx->stream, false));
+  CK(launch_predict_finish(ctx->d_ds, ctx->d_ch, nullptr,
+                           (d.N + kPredWarps - 1) / kPredWarps, chain, kPredNow,
+                           ctx->stream, false));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(mpredict, c.dev.mpred, sizeof(double) * (size_t)d.N * d.S,
+                cudaMemcpyDeviceToHost));
+  return BSG_OK;
+}
+
+bsg_status bsg_get_predictive(bsg_ctx *ctx, int32_t chain, double *qhat,
+                              double *ed_sum, int64_t *npred) {
+  if (!valid_chain(ctx, chain)) return BSG_ERR_INVALID;
+  const Chain &c = ctx->ch[chain];
+  const Dataset &d = ctx->ds[c.dataset];
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const size_t nq = (size_t)d.N * d.S;
+  long long n = 0;
+  double ed = 0.0;
+  if (c.dev.pred_part) {
+    CK(cudaMemcpy(&n, c.dev.npred, sizeof(n), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&ed, c.dev.pred_sums, sizeof(ed), cudaMemcpyDeviceToHost));
+    if (qhat && nq) CK(cudaMemcpy(qhat, c.dev.qhat, sizeof(double) * nq, cudaMemcpyDeviceToHost));
+  } else if (qhat && nq) {
+    std::memset(qhat, 0, sizeof(double) * nq);
+  }
+  if (ed_sum) *ed_sum = ed;
+  if (npred) *npred = n;
+  return BSG_OK;
+}
+
+bsg_status bsg_get_dic(bsg_ctx *ctx, int32_t chain, double *dic) {
+  if (!valid_chain(ctx, chain) || !dic) return BSG_ERR_INVALID;
+  Chain &c = ctx->ch[chain];
+  const Dataset &d = ctx->ds[c.dataset];
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  long long nk = 0, np = 0;
+  CK(cudaMemcpy(&nk, c.dev.nkept, sizeof(nk), cudaMemcpyDeviceToHost));
+  if (c.dev.pred_part) CK(cudaMemcpy(&np, c.dev.npred, sizeof(np), cudaMemcpyDeviceToHost));
+  if (nk < 1 || np < 1)
+    return fail(ctx, BSG_ERR_STATE,
+                "DIC needs kept sweeps with the predictive pass on (bsg_set_predictive)");
+  bsg_status s = build_plan(ctx);
+  if (s) return s;
+  const int chunks = (d.N + kPredThreads - 1) / kPredThreads;
+  CK(launch_predict(d.P, ctx->d_ds, ctx->d_ch, nullptr, c.dev.pred_tiles, chunks,
+                    chain, kPredDE, ctx->stream, false));
+  CK(launch_predict_finish(ctx->d_ds, ctx->d_ch, nullptr,
+                           (d.N + kPredWarps - 1) / kPredWarps, chain, kPredDE,
+                           ctx->stream, false));
+  CK(cudaStreamSynchronize(ctx->stream));
+  double sums[2];
+  CK(cudaMemcpy(sums, c.dev.pred_sums, sizeof(sums), cudaMemcpyDeviceToHost));
+  // mcmc.cpp:966-975
+  const double DE = sums[1];
+  const double ED = -2.0 * sums[0] / (double)np;
+  const double PD = ED - DE;
+  dic[0] = DE;
+  dic[1] = ED;
+  dic[2] = PD;
+  dic[3] = DE + 2.0 * PD;
+  return BSG_OK;
 }
 
 }  // extern "C"

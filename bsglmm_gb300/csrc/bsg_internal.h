@@ -19,6 +19,14 @@ constexpr int kGammaMax = 64;   // Marsaglia-Tsang attempts per gamma draw
 constexpr int kPostThreads = 256;   // block shape of the allocation-free
 constexpr int kPostPerThread = 4;   // Omega pass (bsg_noalloc.cu)
 constexpr int kMaxThreads = 256;    // largest block of the colour kernel
+constexpr int kPredThreads = 128;   // subjects per block of the predictive pass
+constexpr int kPredTile = 1024;     // voxels per block of the predictive pass
+constexpr int kPredWarps = 8;       // subjects (one warp each) per finishing block
+
+// Predictive-pass modes: after each kept sweep (ED and Qhat accumulate), on
+// demand (Mpredict of the current coefficients), or the DE deviance at the
+// posterior means.
+enum : int { kPredKept = 0, kPredNow = 1, kPredDE = 2 };
 
 // Philox counter tags: c3 = chain << 8 | tag.
 enum : uint32_t {
@@ -74,6 +82,15 @@ struct ChainDev {
   long long *nkept;        // kept sweeps accumulated
   int *status;             // sticky error bits of this chain
   int *any_status;         // the context's OR of every chain's bits
+  // DIC / Qhat predictive pass (null until first used)
+  int32_t pred_tiles;      // voxel tiles of kPredTile
+  double *pred_part;       // [tiles][N][max(S,1)] per-tile subject sums
+  double *pred_subj;       // [N] each subject's term of the ED / DE sum
+  double *mpred;           // [N][S] Mpredict of the last pass
+  double *qhat;            // [N][S] Qhat, log scale (mcmc.cpp:223-225)
+  double *pred_sums;       // [2] ED sum over kept sweeps; DE of the last DE pass
+  long long *npred;        // kept sweeps the pass has seen
+  unsigned int *pred_done; // arrival counter of the finishing kernel
 };
 
 // Parity mode: variates supplied by the caller instead of Philox.
@@ -102,5 +119,15 @@ cudaError_t launch_pack(const uint8_t *bytes, int N, int V, int nc,
                         const int32_t *vidx, uint32_t *ybits, int *status,
                         cudaStream_t st);
 bool fused_supported(int P, int lpv, int threads);
+// Predictive pass (bsg_predict.cu).  With map == nullptr the grid is one
+// chain's tiles (blockIdx.x) or subject blocks; otherwise map[blockIdx.x]
+// holds {chain, tile} / {chain, subject block}.  chunks = subject blocks
+// of kPredThreads (gridDim.y).
+cudaError_t launch_predict(int P, const DatasetDev *ds, ChainDev *ch,
+                           const BlockMap *map, int nblocks, int chunks, int chain,
+                           int mode, cudaStream_t st, bool pdl);
+cudaError_t launch_predict_finish(const DatasetDev *ds, ChainDev *ch,
+                                  const BlockMap *map, int nblocks, int chain,
+                                  int mode, cudaStream_t st, bool pdl);
 
 }  // namespace bsg

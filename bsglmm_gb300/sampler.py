@@ -231,6 +231,35 @@ class Sampler:
         self._check(self._L.bsg_reset_accumulators(self._h, chain),
                     "bsg_reset_accumulators")
 
+    # ------------------------------------------------- DIC / Qhat pass --
+    def set_predictive(self, chain: int = 0, enable: bool = True):
+        """Run the DIC / Qhat pass (compute_predictGPU) after every kept
+        sweep of the chain."""
+        self._check(self._L.bsg_set_predictive(self._h, chain, int(bool(enable))),
+                    "bsg_set_predictive")
+
+    def predict(self, chain: int = 0) -> np.ndarray:
+        """Mpredict [N][S] of the current coefficients."""
+        d = self._dims(chain)
+        out = np.zeros((d["N"], d["S"]))
+        self._check(self._L.bsg_predict(self._h, chain, _ptr(out)), "bsg_predict")
+        return out
+
+    def predictive(self, chain: int = 0):
+        """(Qhat [N][S] on the log scale, ED sum, kept sweeps covered)."""
+        d = self._dims(chain)
+        q = np.zeros((d["N"], d["S"]))
+        ed, n = C.c_double(), C.c_int64()
+        self._check(self._L.bsg_get_predictive(self._h, chain, _ptr(q), C.byref(ed),
+                                                C.byref(n)), "bsg_get_predictive")
+        return q, ed.value, n.value
+
+    def dic(self, chain: int = 0) -> dict:
+        """DE, ED, PD and DIC as mcmc.cpp:966-975 reports them."""
+        out = np.zeros(4)
+        self._check(self._L.bsg_get_dic(self._h, chain, _ptr(out)), "bsg_get_dic")
+        return dict(zip(("DE", "ED", "PD", "DIC"), map(float, out)))
+
     def checkpoint(self, chain: int = 0) -> bytes:
         n = int(self._L.bsg_checkpoint_size(self._h, chain))
         buf = np.zeros(n, np.uint8)

@@ -145,6 +145,33 @@ bsg_status bsg_get_maps(bsg_ctx *ctx, int32_t chain, double *spatcoef,
 /* Clears the posterior accumulators and the kept-sweep count. */
 bsg_status bsg_reset_accumulators(bsg_ctx *ctx, int32_t chain);
 
+/* ------------------------------------------------ DIC / Qhat predictive -- */
+/* Replaces compute_predictGPU (covarGPU.cu:1866-1957), which mcmc.cpp:595
+ * calls on every kept sweep, and the DIC of mcmc.cpp:966-975 with
+ * compute_prb_DIC (covar.cpp:442-486).  For subject i and group column g,
+ * Mpredict[i*S+g] = sum over in-mask v of log P(Y_iv | eta), eta =
+ * beta_vg + beta_WM WM_v + sum_{p>=S} beta_vp X_pi, P(Y=1) the A&S 26.2.17
+ * normal CDF.  All need S >= 1.
+ *
+ * bsg_set_predictive: when enabled, each kept sweep also runs the pass
+ * (two more launches per sweep and P group, inside the graph segments) and
+ * accumulates ED = sum over kept sweeps of sum_i Mpredict[i*S + own_i]
+ * (own_i = the first nonzero group column of subject i, else 0) and Qhat
+ * (log scale, covarGPU.cu:1937-1953).  Off by default.  Cleared by
+ * bsg_reset_accumulators; kept in checkpoints. */
+bsg_status bsg_set_predictive(bsg_ctx *ctx, int32_t chain, int32_t enable);
+/* Mpredict [N][S] of the chain's current coefficients (does not touch ED
+ * or Qhat). */
+bsg_status bsg_predict(bsg_ctx *ctx, int32_t chain, double *mpredict);
+/* Qhat [N][S] (may be NULL), the ED sum and the number of kept sweeps it
+ * covers. */
+bsg_status bsg_get_predictive(bsg_ctx *ctx, int32_t chain, double *qhat,
+                              double *ed_sum, int64_t *npred);
+/* dic[4] = {DE, ED, PD, DIC} as mcmc.cpp:966-975 prints them: DE = -2 sum
+ * log P(Y | posterior-mean coefficients), ED = -2 (ED sum) / npred,
+ * PD = ED - DE, DIC = DE + 2 PD.  BSG_ERR_STATE without kept sweeps. */
+bsg_status bsg_get_dic(bsg_ctx *ctx, int32_t chain, double *dic);
+
 /* ------------------------------------------------- checkpoint / tuning -- */
 /* A chain's complete state: coefficients, Omega, sweep counters, posterior
  * sums, Philox key and chain id.  Counter-based variates make a restored

@@ -527,6 +527,71 @@ void orc_compute_prb(const orc_problem *pb, double beta_wm,
   }
 }
 
+/* log of the A&S probability (covar.cpp:327-348) of the observed outcome:
+ * log PhiAS(eta) for y = 1, log PhiAS(-eta) = log(1 - PhiAS(eta)) for
+ * y = 0 (the A&S form satisfies PhiAS(-x) = 1 - PhiAS(x) exactly).  On the
+ * tail side log(c t poly(t)) - eta^2 / 2 is taken without forming exp. */
+double orc_loglik_as(double eta, int y) {
+  const double b1 = 0.319381530, b2 = -0.356563782, b3 = 1.781477937;
+  const double b4 = -1.821255978, b5 = 1.330274429, p = 0.2316419;
+  const double c = 0.39894228;
+  double ax = fabs(eta);
+  double t = 1.0 / (1.0 + p * ax);
+  double r = c * t * (t * (t * (t * (t * b5 + b4) + b3) + b2) + b1);
+  double h = 0.5 * eta * eta;
+  int tail = y ? (eta < 0.0) : (eta >= 0.0);
+  return tail ? log(r) - h : log1p(-r * exp(-h));
+}
+
+/* compute_predictGPU (covarGPU.cu:1866-1903) with ProbSDNormGPU_prediction
+ * (covarGPU.cu:1783-1812) and reduce_for_Mpredict (covarGPU.cu:1826-1864):
+ *   mpredict[i*S + g] = sum over in-mask v of log P(Y_iv | eta_igv),
+ *   eta_igv = beta_vg + beta_WM WM_v + sum_{p >= S} beta_vp X_pi,
+ * i.e. subject i's prediction as a member of group column g.  The
+ * reference's y log(p + 1e-35) + (1 - y) log(1 - p + 1e-35) in FP32 is the
+ * same quantity up to its guard and its cancellation when 1 - p < 2^-24. */
+void orc_predict(const orc_problem *pb, double beta_wm, const double *spatcoef,
+                 double *mpredict) {
+  int N = pb->N, P = pb->P, S = pb->S, V = pb->V, Vp = pb->Vp;
+  for (int i = 0; i < N * S; ++i) mpredict[i] = 0.0;
+  for (int q = 0; q < pb->nsize; ++q) {
+    if (!pb->msk[q]) continue;
+    int v = pb->idx[q], sc = pb->idxsc[q];
+    double bwm = beta_wm * pb->wm[v];
+    for (int i = 0; i < N; ++i) {
+      double rest = bwm;
+      for (int p = S; p < P; ++p)
+        rest += spatcoef[(size_t)p * Vp + sc] * (double)pb->covar[(size_t)p * N + i];
+      int y = pb->data[(size_t)i * V + v] != 0;
+      for (int g = 0; g < S; ++g)
+        mpredict[(size_t)i * S + g] +=
+            orc_loglik_as(spatcoef[(size_t)g * Vp + sc] + rest, y);
+    }
+  }
+}
+
+/* compute_prb_DIC (covar.cpp:442-486), probit branch, as written there:
+ *   DE = -2 sum_i sum_v [y log(x + DBL_MIN) + (1 - y) log(1 - x + DBL_MIN)],
+ *   x = PhiAS((float)(sum_p mean_vp X_pi + mwm_v))
+ * at the posterior means mean[p*V + v] (all P columns with the subject's own
+ * covariates) and mwm[v] = mean of beta_WM WM_v.  The reference rounds eta
+ * to float before its FP64 A&S evaluation, and its 1 - x cancels for
+ * eta > 5 (relative error 1e-16 / (1 - x)); both are kept here. */
+double orc_dic_de(const orc_problem *pb, const double *mean, const double *mwm) {
+  int N = pb->N, P = pb->P, V = pb->V;
+  double de = 0.0;
+  for (int i = 0; i < N; ++i)
+    for (int v = 0; v < V; ++v) {
+      double y = 0.0;
+      for (int p = 0; p < P; ++p)
+        y += mean[(size_t)p * V + v] * (double)pb->covar[(size_t)p * N + i];
+      double x = orc_prob_sdnorm((double)(float)(y + (mwm ? mwm[v] : 0.0)));
+      int t = pb->data[(size_t)i * V + v];
+      de += t * log(x + DBL_MIN) + (1 - t) * log(1.0 - x + DBL_MIN);
+    }
+  return -2.0 * de;
+}
+
 void orc_col_means(const orc_problem *pb, const double *spatcoef,
                    double *means) {
   for (int p = 0; p < pb->P; ++p) {

@@ -89,6 +89,15 @@ double orc_prob_sdnorm(double x);
 /* covar.cpp:350-364: prb[g*V + v]. */
 void orc_compute_prb(const orc_problem *pb, double beta_wm,
                      const double *spatcoef, double *prb);
+/* log of the A&S probability of outcome y given eta. */
+double orc_loglik_as(double eta, int y);
+/* compute_predictGPU (covarGPU.cu:1783-1903): mpredict[i*S + g], the log
+ * predictive of subject i's outcomes as a member of group column g. */
+void orc_predict(const orc_problem *pb, double beta_wm, const double *spatcoef,
+                 double *mpredict);
+/* compute_prb_DIC (covar.cpp:442-486): DE at the posterior means
+ * mean[p*V + v] with mwm[v] (NULL = 0). */
+double orc_dic_de(const orc_problem *pb, const double *mean, const double *mwm);
 /* Column means (covarGPU.cu:563-583): sum over Vp entries / V. */
 void orc_col_means(const orc_problem *pb, const double *spatcoef,
                    double *means);

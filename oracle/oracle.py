@@ -71,6 +71,9 @@ def lib() -> C.CDLL:
             "orc_prob_sdnorm": (_d, [_d]),
             "orc_compute_prb": (None, [_P, _d, _P, _P]),
             "orc_col_means": (None, [_P, _P, _P]),
+            "orc_loglik_as": (_d, [_d, _i]),
+            "orc_predict": (None, [_P, _d, _P, _P]),
+            "orc_dic_de": (_d, [_P, _P, _P]),
             "orc_chain_run": (_i, [_P, _P, _i64, _i64, _P, _P, _P, _P, _P, _P]),
             "orc_port_new": (_P, [_P, C.c_uint64, _i]),
             "orc_port_free": (None, [_P]),
@@ -187,6 +190,20 @@ class Problem:
         self._L.orc_col_means(self.h, _p(b), _p(out))
         return out
 
+    def predict(self, spatcoef, beta_wm=0.0) -> np.ndarray:
+        """Mpredict [N][S] of compute_predictGPU (covarGPU.cu:1866-1903)."""
+        b = np.ascontiguousarray(spatcoef, dtype=np.float64)
+        out = np.zeros((self.N, self.S))
+        self._L.orc_predict(self.h, beta_wm, _p(b), _p(out))
+        return out
+
+    def dic_de(self, mean, mwm=None) -> float:
+        """DE of compute_prb_DIC (covar.cpp:442-486) at the posterior means
+        mean [P][V] and mwm [V] (None = 0)."""
+        m = np.ascontiguousarray(mean, dtype=np.float64)
+        w = None if mwm is None else np.ascontiguousarray(mwm, dtype=np.float64)
+        return self._L.orc_dic_de(self.h, _p(m), _p(w))
+
     def sweep_supplied(self, spatcoef, omega, ubits, normals, chi2, wnorm,
                        form=0, beta_wm=0.0):
         """One full sweep (Z, beta both colours, Omega) from supplied
@@ -219,6 +236,30 @@ class Problem:
             prb = sp[: self.S] / T
         return dict(beta=b, omega=om, mean=mean, var=var, prb=prb,
                     sum=s1, sumsq=s2, nkept=T, err=err)
+
+
+def subtypes(covar, S: int) -> np.ndarray:
+    """compute_predictGPU's group of each subject (covarGPU.cu:1929-1935):
+    the first of the S group columns that is nonzero, else 0."""
+    c = np.asarray(covar)[:S] != 0
+    return np.where(c.any(0), np.argmax(c, axis=0), 0)
+
+
+def qhat_update(qhat, mpredict, sub, first: bool) -> None:
+    """The host part of compute_predictGPU (covarGPU.cu:1937-1953), in place:
+    d = Mpredict[i][g] - Mpredict[i][sub_i]; on the first kept sweep
+    Qhat[i][0] = d_0 and Qhat[i][g] = log(exp(Qhat) + exp(d_g)) for g >= 1
+    (Qhat starts at 0, mcmc.cpp:223-225); afterwards the log-sum for all g."""
+    mp = np.asarray(mpredict, dtype=np.float64)
+    n = mp.shape[0]
+    d = mp - mp[np.arange(n), np.asarray(sub)][:, None]
+    for i in range(n):
+        for g in range(mp.shape[1]):
+            if first and g == 0:
+                qhat[i, 0] = d[i, 0]
+                continue
+            m = max(d[i, g], qhat[i, g])
+            qhat[i, g] = np.log(np.exp(qhat[i, g] - m) + np.exp(d[i, g] - m)) + m
 
 
 class Port:
@@ -272,6 +313,8 @@ class _Ref:
             getattr(L, n).argtypes = a
         L.ref_prob_sdnorm.argtypes = [_d]
         L.ref_prob_sdnorm.restype = _d
+        L.ref_compute_prb_dic.argtypes = [_P, _P, _P, _P]
+        L.ref_compute_prb_dic.restype = _d
         L.ref_cholesky_decomp.restype = _i
 
     def xtx(self):
@@ -308,6 +351,27 @@ class _Ref:
 
     def prob_sdnorm(self, x: float) -> float:
         return self._L.ref_prob_sdnorm(x)
+
+    def compute_prb_dic(self, mean, mwm=None) -> float:
+        """The reference's compute_prb_DIC on posterior means [P][V]."""
+        pb = self.pb
+        R = pb.X * pb.Y * pb.Z
+        lat = self._keep
+        inmask = lat["idx"] >= 0
+        # unpadded grid index of each compact voxel v
+        pad = np.nonzero(inmask)[0]
+        i = pad % (pb.X + 2) - 1
+        j = (pad // (pb.X + 2)) % (pb.Y + 2) - 1
+        k = pad // ((pb.X + 2) * (pb.Y + 2)) - 1
+        grid = i + pb.X * j + pb.X * pb.Y * k
+        v = lat["idx"][pad]
+        mc = np.zeros((pb.P, R))
+        mc[:, grid] = np.asarray(mean, dtype=np.float64)[:, v]
+        mw = np.zeros(R)
+        if mwm is not None:
+            mw[grid] = np.asarray(mwm, dtype=np.float64)[v]
+        return self._L.ref_compute_prb_dic(_p(mc), _p(mw), _p(pb.covar),
+                                           _p(pb.data))
 
 
 class RefSupplied(_Ref):

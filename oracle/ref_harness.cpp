@@ -47,6 +47,8 @@ void updateSpatCoef(float *, float *, float *, float *, float *, float *,
                     unsigned char *, float, float *, unsigned long *);
 void updateSpatCoefPrec(float *, float *, unsigned char *, unsigned long *);
 void compute_prb(float *, float *, float *, float, float *, unsigned char *);
+double compute_prb_DIC(double *, double *, float *, unsigned char *,
+                       unsigned char *, int);
 double ProbSDNorm(const double x);
 int cholesky_decomp(double *A, int num_col);
 void cholesky_invert(int len, double *H);
@@ -192,6 +194,14 @@ void ref_compute_prb(float *prb, const float *spatcoef, const float *wm,
 }
 
 double ref_prob_sdnorm(double x) { return ProbSDNorm(x); }
+
+/* covar.cpp:442-486: DE from the posterior-mean maps mcov[p][X*Y*Z] and
+ * mwm[X*Y*Z] on the unpadded grid (x fastest), outcomes data[i*V + v]. */
+double ref_compute_prb_dic(double *mcov, double *mwm, float *covar,
+                           const uint8_t *data) {
+  return compute_prb_DIC(mcov, mwm, covar, (unsigned char *)data,
+                         g_mskpad.data(), NROW * NCOL * NDEPTH);
+}
 
 int ref_cholesky_decomp(double *A, int n) { return cholesky_decomp(A, n); }
 void ref_cholesky_invert(double *H, int n) { cholesky_invert(n, H); }

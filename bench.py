@@ -428,6 +428,69 @@ def run_batched(args, rank, world, local):
         print(json.dumps(line))
 
 
+def run_dic(args, rank, world, local):
+    """The DIC / Qhat predictive pass on the brain-sized study with two
+    indicator group columns (the two arms of the +-0.5 group column): device
+    time per kept sweep with the pass on against off (every sweep kept, L2
+    flushed before each sweep), and the on-demand pass."""
+    import torch
+    import bsglmm_gb300 as bsg
+    from bsglmm_gb300 import synth
+    torch.cuda.set_device(local)
+    study = synth.config1(seed=1)
+    covar = study.covar.copy()
+    arm = covar[1] > 0
+    covar[0], covar[1] = ~arm, arm
+    N, P, V, S = study.N, study.P, study.V, 2
+    flushbuf = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+    s = bsg.Sampler(local)
+    ds = s.add_dataset(study.mask, covar, study.data, S)
+    ch = s.add_chain(ds, seed=chain_seed(rank), burnin=0, thin=1)
+
+    def timed(steps):
+        ms = []
+        for _ in range(steps):
+            flush_l2(flushbuf)
+            torch.cuda.synchronize()
+            ms.append(s.run_timed(1))
+        s.sync()
+        return float(np.median(ms))
+
+    for _ in range(args.warmup):
+        s.run_timed(1)
+    with Clocks(local) as clk:
+        off = timed(args.steps)
+        s.set_predictive(ch, True)
+        for _ in range(args.warmup):
+            s.run_timed(1)
+        on = timed(args.steps)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            s.predict(ch)
+        call = (time.perf_counter() - t0) / args.steps
+    q, ed, npred = s.predictive(ch)
+    dic = s.dic(ch)
+    s.close()
+    evals = N * V * S
+    added = on - off
+    line = {
+        "metric": "subject-voxel-group log predictive evaluations/s (DIC/Qhat pass)",
+        "value": evals / (added * 1e-3), "unit": "evaluations/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": added,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (f64 sums)", "data": "synthetic",
+        "config": {"workload": "brain-sized study, 91x109x91 grid, N=1000, P=5, "
+                               "two indicator group columns (S=2)",
+                   "V": V, "N": N, "P": P, "S": S,
+                   "l2": "flushed between timed sweeps", "timing": "device, median"},
+        "sweep_ms_off": off, "sweep_ms_on_every_sweep_kept": on,
+        "predict_call_ms": call * 1e3, "gpu_launches_per_kept_sweep": 2,
+        "npred": npred, "dic": dic, "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -437,9 +500,13 @@ def main():
     ap.add_argument("--lpv", type=int, default=0)
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="brain", choices=["brain"] + sorted(BATCHED))
+    ap.add_argument("--workload", default="brain",
+                    choices=["brain", "dic"] + sorted(BATCHED))
     args = ap.parse_args()
     rank, world, local = dist_env()
+    if args.workload == "dic" and args.impl == "ours":
+        run_dic(args, rank, world, local)
+        return
     if args.workload != "brain" and args.impl == "ours":
         run_batched(args, rank, world, local)
         return

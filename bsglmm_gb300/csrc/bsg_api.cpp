@@ -45,11 +45,16 @@ struct Group {
   int P = 0;
   std::vector<BlockMap> map[2];
   BlockMap *d_map[2] = {nullptr, nullptr};
-  // predictive pass of the group's chains that have it on: {chain, tile}
-  // blocks, {chain, subject block} finishing blocks, subject chunks
-  std::vector<BlockMap> pmap, fmap;
-  BlockMap *d_pmap = nullptr, *d_fmap = nullptr;
-  int pchunks = 0;
+  // predictive pass of the group's chains that have it on, one launch pair
+  // per number of group columns S: {chain, tile} blocks, {chain, subject
+  // block} finishing blocks, subject chunks
+  struct Pred {
+    int S = 0;
+    std::vector<BlockMap> pmap, fmap;
+    BlockMap *d_pmap = nullptr, *d_fmap = nullptr;
+    int pchunks = 0;
+  };
+  std::vector<Pred> pred;
 };
 
 // Small per-chain counters of the predictive pass.
@@ -277,8 +282,10 @@ bsg_status build_plan(bsg_ctx *ctx) {
                 cudaMemcpyHostToDevice));
   for (auto &g : ctx->groups) {
     for (int c = 0; c < 2; ++c) dfree(ctx, g.d_map[c]);
-    dfree(ctx, g.d_pmap);
-    dfree(ctx, g.d_fmap);
+    for (auto &pr : g.pred) {
+      dfree(ctx, pr.d_pmap);
+      dfree(ctx, pr.d_fmap);
+    }
   }
   ctx->groups.clear();
   for (size_t ci = 0; ci < ctx->ch.size(); ++ci) {
@@ -294,9 +301,17 @@ bsg_status build_plan(bsg_ctx *ctx) {
     for (int c = 0; c < 2; ++c) map_chain(g->map[c], (int)ci, (int)d.vox[c].size(), vpb, c);
     if (ctx->ch[ci].pred_on) {
       const ChainDev &cv = ctx->ch[ci].dev;
-      for (int t = 0; t < cv.pred_tiles; ++t) g->pmap.push_back({(int32_t)ci, (int32_t)t});
-      for (int b = 0; b * kPredWarps < d.N; ++b) g->fmap.push_back({(int32_t)ci, (int32_t)b});
-      g->pchunks = std::max(g->pchunks, (d.N + kPredThreads - 1) / kPredThreads);
+      Group::Pred *pr = nullptr;
+      for (auto &q : g->pred)
+        if (q.S == d.S) pr = &q;
+      if (!pr) {
+        g->pred.push_back(Group::Pred());
+        pr = &g->pred.back();
+        pr->S = d.S;
+      }
+      for (int t = 0; t < cv.pred_tiles; ++t) pr->pmap.push_back({(int32_t)ci, (int32_t)t});
+      for (int b = 0; b * kPredWarps < d.N; ++b) pr->fmap.push_back({(int32_t)ci, (int32_t)b});
+      pr->pchunks = std::max(pr->pchunks, (d.N + kPredThreads - 1) / kPredThreads);
     }
   }
   for (auto &g : ctx->groups) {
@@ -304,10 +319,10 @@ bsg_status build_plan(bsg_ctx *ctx) {
       g.d_map[c] = upload(ctx, g.map[c].data(), g.map[c].size(), &e);
       CK(e);
     }
-    if (!g.pmap.empty()) {
-      g.d_pmap = upload(ctx, g.pmap.data(), g.pmap.size(), &e);
+    for (auto &pr : g.pred) {
+      pr.d_pmap = upload(ctx, pr.pmap.data(), pr.pmap.size(), &e);
       CK(e);
-      g.d_fmap = upload(ctx, g.fmap.data(), g.fmap.size(), &e);
+      pr.d_fmap = upload(ctx, pr.fmap.data(), pr.fmap.size(), &e);
       CK(e);
     }
   }
@@ -334,12 +349,12 @@ cudaError_t enqueue_group(bsg_ctx *ctx, const Group &g, cudaStream_t st) {
                      g.d_map[c], (int)g.map[c].size(), c, sup, st, ctx->pdl);
     if (e != cudaSuccess) return e;
   }
-  if (!g.pmap.empty()) {
+  for (const auto &pr : g.pred) {
     // DIC / Qhat pass; its blocks return at once unless the sweep is kept
-    e = launch_predict(g.P, ctx->d_ds, ctx->d_ch, g.d_pmap, (int)g.pmap.size(),
-                       g.pchunks, 0, kPredKept, st, ctx->pdl);
+    e = launch_predict(g.P, pr.S, ctx->d_ds, ctx->d_ch, pr.d_pmap, (int)pr.pmap.size(),
+                       pr.pchunks, 0, kPredKept, st, ctx->pdl);
     if (e != cudaSuccess) return e;
-    e = launch_predict_finish(ctx->d_ds, ctx->d_ch, g.d_fmap, (int)g.fmap.size(), 0,
+    e = launch_predict_finish(ctx->d_ds, ctx->d_ch, pr.d_fmap, (int)pr.fmap.size(), 0,
                               kPredKept, st, ctx->pdl);
     if (e != cudaSuccess) return e;
   }
@@ -407,8 +422,17 @@ PredCounters *pred_counters_of(const Chain &c) {
 bsg_status ensure_pred(bsg_ctx *ctx, Chain &c) {
   if (c.dev.pred_part) return BSG_OK;
   const Dataset &d = ctx->ds[c.dataset];
+  // Tiles sized so that one chain's grid (tiles x subject chunks) is about
+  // one wave of resident blocks.
   const int ntot = (int)(d.vox[0].size() + d.vox[1].size());
-  const int T = std::max(1, (ntot + kPredTile - 1) / kPredTile);
+  const int chunks = (d.N + kPredThreads - 1) / kPredThreads;
+  int sms = 1;
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  const int cap = sms * predict_blocks_per_sm(d.P, std::max(d.S, 1));
+  const int want = std::max(1, cap / std::max(chunks, 1));
+  int tile = (ntot + want - 1) / want;
+  tile = std::max(kPredThreads, (tile + kPredThreads - 1) / kPredThreads * kPredThreads);
+  const int T = std::max(1, (ntot + tile - 1) / tile);
   const size_t N = (size_t)d.N, G = (size_t)std::max(d.S, 1);
   cudaError_t e;
   ChainDev &cv = c.dev;
@@ -431,6 +455,7 @@ bsg_status ensure_pred(bsg_ctx *ctx, Chain &c) {
   cv.npred = &pc->npred;
   cv.pred_done = &pc->done;
   cv.pred_tiles = T;
+  cv.pred_tile = tile;
   cv.pred_part = part;
   ctx->plan_valid = false;  // the device copy of the chain changed
   return BSG_OK;
@@ -785,9 +810,10 @@ int64_t bsg_launches_per_sweep(const bsg_ctx *ctx) {
   if (!ctx) return 0;
   std::vector<int> ps, pp;
   for (auto &c : ctx->ch) {
-    const int P = ctx->ds[c.dataset].P;
+    const Dataset &d = ctx->ds[c.dataset];
+    const int P = d.P, PS = d.P * 16 + d.S;
     if (std::find(ps.begin(), ps.end(), P) == ps.end()) ps.push_back(P);
-    if (c.pred_on && std::find(pp.begin(), pp.end(), P) == pp.end()) pp.push_back(P);
+    if (c.pred_on && std::find(pp.begin(), pp.end(), PS) == pp.end()) pp.push_back(PS);
   }
   return (int64_t)(2 * ps.size() + 2 * pp.size());
 }
@@ -1247,7 +1273,7 @@ bsg_status bsg_predict(bsg_ctx *ctx, int32_t chain, double *mpredict) {
   if (s) return s;
   if ((s = build_plan(ctx))) return s;
   const int chunks = (d.N + kPredThreads - 1) / kPredThreads;
-  CK(launch_predict(d.P, ctx->d_ds, ctx->d_ch, nullptr, c.dev.pred_tiles, chunks,
+  CK(launch_predict(d.P, d.S, ctx->d_ds, ctx->d_ch, nullptr, c.dev.pred_tiles, chunks,
                     chain, kPredNow, ctx->stream, false));
   CK(launch_predict_finish(ctx->d_ds, ctx->d_ch, nullptr,
                            (d.N + kPredWarps - 1) / kPredWarps, chain, kPredNow,
@@ -1295,7 +1321,7 @@ bsg_status bsg_get_dic(bsg_ctx *ctx, int32_t chain, double *dic) {
   bsg_status s = build_plan(ctx);
   if (s) return s;
   const int chunks = (d.N + kPredThreads - 1) / kPredThreads;
-  CK(launch_predict(d.P, ctx->d_ds, ctx->d_ch, nullptr, c.dev.pred_tiles, chunks,
+  CK(launch_predict(d.P, d.S, ctx->d_ds, ctx->d_ch, nullptr, c.dev.pred_tiles, chunks,
                     chain, kPredDE, ctx->stream, false));
   CK(launch_predict_finish(ctx->d_ds, ctx->d_ch, nullptr,
                            (d.N + kPredWarps - 1) / kPredWarps, chain, kPredDE,

@@ -20,7 +20,6 @@ constexpr int kPostThreads = 256;   // block shape of the allocation-free
 constexpr int kPostPerThread = 4;   // Omega pass (bsg_noalloc.cu)
 constexpr int kMaxThreads = 256;    // largest block of the colour kernel
 constexpr int kPredThreads = 128;   // subjects per block of the predictive pass
-constexpr int kPredTile = 1024;     // voxels per block of the predictive pass
 constexpr int kPredWarps = 8;       // subjects (one warp each) per finishing block
 
 // Predictive-pass modes: after each kept sweep (ED and Qhat accumulate), on
@@ -83,7 +82,8 @@ struct ChainDev {
   int *status;             // sticky error bits of this chain
   int *any_status;         // the context's OR of every chain's bits
   // DIC / Qhat predictive pass (null until first used)
-  int32_t pred_tiles;      // voxel tiles of kPredTile
+  int32_t pred_tiles;      // voxel tiles of the predictive pass
+  int32_t pred_tile;       // voxels per tile (a multiple of kPredThreads)
   double *pred_part;       // [tiles][N][max(S,1)] per-tile subject sums
   double *pred_subj;       // [N] each subject's term of the ED / DE sum
   double *mpred;           // [N][S] Mpredict of the last pass
@@ -123,9 +123,11 @@ bool fused_supported(int P, int lpv, int threads);
 // chain's tiles (blockIdx.x) or subject blocks; otherwise map[blockIdx.x]
 // holds {chain, tile} / {chain, subject block}.  chunks = subject blocks
 // of kPredThreads (gridDim.y).
-cudaError_t launch_predict(int P, const DatasetDev *ds, ChainDev *ch,
+cudaError_t launch_predict(int P, int S, const DatasetDev *ds, ChainDev *ch,
                            const BlockMap *map, int nblocks, int chunks, int chain,
                            int mode, cudaStream_t st, bool pdl);
+// Resident blocks per SM of predict_kernel<P, S>, for sizing its tiles.
+int predict_blocks_per_sm(int P, int S);
 cudaError_t launch_predict_finish(const DatasetDev *ds, ChainDev *ch,
                                   const BlockMap *map, int nblocks, int chain,
                                   int mode, cudaStream_t st, bool pdl);

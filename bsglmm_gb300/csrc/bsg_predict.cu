@@ -10,11 +10,13 @@
 // reference launches 2 + S kernels and a blocking copy per subject; here one
 // launch covers every subject and voxel and a second reduces the tiles.
 //
-// predict_kernel: a block takes 128 subjects (one per thread, the design
-// row in registers) and a tile of 1024 voxels staged 128 at a time in shared
-// memory (coefficients as float4 pairs, beta_WM WM_v, and each warp's
-// 32-subject outcome word per voxel).  Per-thread sums are FP32 over 32
-// voxels, then FP64; each block writes its [subjects][columns] partials.
+// predict_kernel<P, S>: a block takes 128 subjects (one per thread, the
+// design row in registers) and a tile of voxels, sized on the host so that
+// the grid is one wave, staged 128 at a time in shared memory (the voxel's
+// coefficients and beta_WM WM_v as float4s, and each warp's 32-subject
+// outcome word).  The outcome enters as a sign flip of eta.  Per-thread
+// sums are FP32 (log2 units) over 32 voxels, then FP64; each block writes
+// its [subjects][columns] partials.
 //
 // predict_finish_kernel: one warp per subject sums the tile partials in a
 // fixed order (lane l takes tiles l, l + 32, ...; xor-shuffle tree), so the
@@ -37,20 +39,24 @@ namespace {
 constexpr int kPredSub = 128;  // voxels staged per pass (one per thread)
 static_assert(kPredSub == kPredThreads, "staging uses one voxel per thread");
 
-// ln P(Y = y | eta) under A&S 26.2.17, FP32.
-__device__ __forceinline__ float loglik_as(float eta, uint32_t y) {
-  const float b1 = 0.319381530f, b2 = -0.356563782f, b3 = 1.781477937f;
-  const float b4 = -1.821255978f, b5 = 1.330274429f, p = 0.2316419f;
-  const float c = 0.39894228f;
-  const float ax = fabsf(eta);
-  const float t = rcp_approx(fmaf(p, ax, 1.0f));
-  const float r = c * t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, b5, b4), b3), b2), b1);
-  const float h = 0.5f * eta * eta;
-  // tail side: Y = 1 with eta < 0, or Y = 0 with eta >= 0
-  const bool tail = y ? (eta < 0.f) : (eta >= 0.f);
-  const float e = ex2_approx(h * -1.44269504f);
-  const float u = tail ? r : fmaf(-r, e, 1.0f);
-  return fmaf(lg2_approx(u), 0.693147181f, tail ? -h : 0.f);
+// A&S 26.2.17 with 1/sqrt(2 pi) folded in: c * (b1 t + ... + b5 t^5).
+constexpr float kA1 = 0.39894228f * 0.319381530f;
+constexpr float kA2 = 0.39894228f * -0.356563782f;
+constexpr float kA3 = 0.39894228f * 1.781477937f;
+constexpr float kA4 = 0.39894228f * -1.821255978f;
+constexpr float kA5 = 0.39894228f * 1.330274429f;
+
+// log2 P(Y | eta) under A&S 26.2.17, FP32, for a = eta with its sign bit
+// flipped when Y = 0: the observed outcome lies on the tail side iff a < 0.
+// Tail side: log2(c t poly(t)) - eta^2 / (2 ln 2); other side:
+// log2(1 - c t poly(t) exp(-eta^2 / 2)).
+__device__ __forceinline__ float log2lik_as(float a) {
+  const float t = rcp_approx(fmaf(0.2316419f, fabsf(a), 1.0f));
+  const float r = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, kA5, kA4), kA3), kA2), kA1);
+  const float w = (a * -0.721347520f) * a;  // -eta^2 / 2 in log2 units
+  const bool tail = a < 0.f;
+  const float u = tail ? r : fmaf(-r, ex2_approx(w), 1.0f);
+  return lg2_approx(u) + (tail ? w : 0.f);
 }
 
 __device__ __forceinline__ bool predict_gate(const ChainDev &ch, int mode) {
@@ -59,10 +65,13 @@ __device__ __forceinline__ bool predict_gate(const ChainDev &ch, int mode) {
   return s > ch.burnin && (s % (ch.thin > 0 ? ch.thin : 1)) == 0;
 }
 
-template <int P>
+// P covariates, the first S of them group columns.  Shared row per voxel:
+// P coefficients then beta_WM WM_v, padded to float4s.
+template <int P, int S>
 __global__ void __launch_bounds__(kPredThreads)
     predict_kernel(const DatasetDev *__restrict__ dsv, ChainDev *__restrict__ chv,
                    const BlockMap *__restrict__ map, int chain, int mode) {
+  constexpr int Q = (P + 1 + 3) / 4;  // float4s per staged voxel
   // Coefficients of this sweep are final once the previous kernel is done.
   cudaGridDependencySynchronize();
   cudaTriggerProgrammaticLaunchCompletion();
@@ -70,29 +79,28 @@ __global__ void __launch_bounds__(kPredThreads)
   const int tile = map ? map[blockIdx.x].start : (int)blockIdx.x;
   const ChainDev &ch = chv[cidx];
   const DatasetDev &d = dsv[ch.dataset];
-  const int N = d.N, S = d.S, Vp = d.Vp, V = d.V;
+  const int N = d.N, Vp = d.Vp, V = d.V;
   const int i0 = blockIdx.y * kPredThreads;
   if (i0 >= N || !predict_gate(ch, mode)) return;  // uniform per block
-  const int G = mode == kPredDE ? 1 : S;
+  const bool de = mode == kPredDE;
   const int n0 = d.n[0], ntot = n0 + d.n[1];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int i = i0 + tid;
   const int word = i0 / 32 + warp;  // this warp's 32-subject outcome word
+  const int tw = ch.pred_tile;      // voxels per tile
 
-  __shared__ float4 Bs[kPredSub][2];
-  __shared__ float Bw[kPredSub];
+  __shared__ float4 Bs[kPredSub][Q];
   __shared__ uint32_t Ys[kPredThreads / 32][kPredSub];
 
   float x[P];
 #pragma unroll
   for (int p = 0; p < P; ++p) x[p] = i < N ? d.covar[(size_t)p * N + i] : 0.f;
-  double acc[P];
+  double acc[S];
 #pragma unroll
-  for (int g = 0; g < P; ++g) acc[g] = 0.0;
-  const double inv_nk =
-      mode == kPredDE ? 1.0 / (double)(*ch.nkept > 0 ? *ch.nkept : 1) : 0.0;
+  for (int g = 0; g < S; ++g) acc[g] = 0.0;
+  const double inv_nk = de ? 1.0 / (double)(*ch.nkept > 0 ? *ch.nkept : 1) : 0.0;
 
-  const int t0 = tile * kPredTile, t1 = min(t0 + kPredTile, ntot);
+  const int t0 = tile * tw, t1 = min(t0 + tw, ntot);
   for (int q0 = t0; q0 < t1; q0 += kPredSub) {
     const int nsub = min(kPredSub, t1 - q0);
     __syncthreads();
@@ -100,19 +108,19 @@ __global__ void __launch_bounds__(kPredThreads)
       const int pos = q0 + tid;
       const int c = pos < n0 ? 0 : 1, j = c ? pos - n0 : pos;
       const int sc = d.nb[c][j], v = d.vidx[c][j];
-      float b[8];
+      float b[4 * Q];
 #pragma unroll
-      for (int p = 0; p < 8; ++p) {
-        if (p >= P)
-          b[p] = 0.f;
-        else if (mode == kPredDE)
-          b[p] = (float)(ch.acc_sum[(size_t)p * V + v] * inv_nk);
+      for (int p = 0; p < 4 * Q; ++p) {
+        if (p < P)
+          b[p] = de ? (float)(ch.acc_sum[(size_t)p * V + v] * inv_nk)
+                    : ch.beta[(size_t)p * Vp + sc];
         else
-          b[p] = ch.beta[(size_t)p * Vp + sc];
+          b[p] = 0.f;
       }
-      Bs[tid][0] = make_float4(b[0], b[1], b[2], b[3]);
-      Bs[tid][1] = make_float4(b[4], b[5], b[6], b[7]);
-      Bw[tid] = ch.beta_wm * (d.wm ? d.wm[v] : 1.f);
+      b[P] = ch.beta_wm * (d.wm ? d.wm[v] : 1.f);
+#pragma unroll
+      for (int u = 0; u < Q; ++u)
+        Bs[tid][u] = make_float4(b[4 * u], b[4 * u + 1], b[4 * u + 2], b[4 * u + 3]);
     }
     if (word < d.W) {
       for (int k = lane; k < nsub; k += 32) {
@@ -123,39 +131,46 @@ __global__ void __launch_bounds__(kPredThreads)
     }
     __syncthreads();
     if (i < N) {
+      const int sh = 31 - lane;  // brings this subject's bit to the sign
       for (int k0 = 0; k0 < nsub; k0 += 32) {
         const int k1 = min(k0 + 32, nsub);
-        float s32[P];
+        float s32[S];
 #pragma unroll
-        for (int g = 0; g < P; ++g) s32[g] = 0.f;
+        for (int g = 0; g < S; ++g) s32[g] = 0.f;
+#pragma unroll 2
         for (int k = k0; k < k1; ++k) {
-          const float4 u0 = Bs[k][0], u1 = Bs[k][1];
-          const float b[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
-          const uint32_t y = (Ys[warp][k] >> lane) & 1u;
-          if (mode == kPredDE) {
-            float eta = Bw[k];
+          float b[4 * Q];
+#pragma unroll
+          for (int u = 0; u < Q; ++u) {
+            const float4 f = Bs[k][u];
+            b[4 * u] = f.x, b[4 * u + 1] = f.y, b[4 * u + 2] = f.z, b[4 * u + 3] = f.w;
+          }
+          // sign mask: flips eta's sign when Y = 0
+          const uint32_t ymask = ~(Ys[warp][k] << sh) & 0x80000000u;
+          if (de) {
+            float eta = b[P];
 #pragma unroll
             for (int p = 0; p < P; ++p) eta = fmaf(b[p], x[p], eta);
-            s32[0] += loglik_as(eta, y);
+            s32[0] += log2lik_as(__uint_as_float(__float_as_uint(eta) ^ ymask));
           } else {
-            float rest = Bw[k];
+            float rest = b[P];
 #pragma unroll
-            for (int p = 0; p < P; ++p)
-              if (p >= S) rest = fmaf(b[p], x[p], rest);
+            for (int p = S; p < P; ++p) rest = fmaf(b[p], x[p], rest);
 #pragma unroll
-            for (int g = 0; g < P; ++g)
-              if (g < S) s32[g] += loglik_as(b[g] + rest, y);
+            for (int g = 0; g < S; ++g)
+              s32[g] += log2lik_as(__uint_as_float(__float_as_uint(b[g] + rest) ^ ymask));
           }
         }
 #pragma unroll
-        for (int g = 0; g < P; ++g) acc[g] += (double)s32[g];
+        for (int g = 0; g < S; ++g) acc[g] = fma((double)s32[g], 0.6931471805599453, acc[g]);
       }
     }
   }
   if (i < N) {
+    const int G = de ? 1 : S;
     double *out = ch.pred_part + ((size_t)tile * N + i) * G;
 #pragma unroll
-    for (int g = 0; g < P; ++g)
+    for (int g = 0; g < S; ++g)
       if (g < G) out[g] = acc[g];
   }
 }
@@ -260,10 +275,10 @@ __global__ void __launch_bounds__(kPredWarps * 32)
   }
 }
 
-template <int P>
-cudaError_t launch_predict_p(const DatasetDev *ds, ChainDev *ch, const BlockMap *map,
-                             int nblocks, int chunks, int chain, int mode,
-                             cudaStream_t st, bool pdl) {
+template <int P, int S>
+cudaError_t launch_predict_ps(const DatasetDev *ds, ChainDev *ch, const BlockMap *map,
+                              int nblocks, int chunks, int chain, int mode,
+                              cudaStream_t st, bool pdl) {
   cudaLaunchConfig_t cfg{};
   cfg.gridDim = dim3(nblocks, chunks);
   cfg.blockDim = dim3(kPredThreads);
@@ -273,28 +288,66 @@ cudaError_t launch_predict_p(const DatasetDev *ds, ChainDev *ch, const BlockMap 
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = pdl ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, predict_kernel<P>, ds, ch, map, chain, mode);
+  return cudaLaunchKernelEx(&cfg, predict_kernel<P, S>, ds, ch, map, chain, mode);
 }
 
-}  // namespace
+template <int P, int S>
+int predict_blocks_per_sm_ps() {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, predict_kernel<P, S>,
+                                                    kPredThreads, 0) != cudaSuccess)
+    return 1;
+  return n > 0 ? n : 1;
+}
 
-cudaError_t launch_predict(int P, const DatasetDev *ds, ChainDev *ch,
-                           const BlockMap *map, int nblocks, int chunks, int chain,
-                           int mode, cudaStream_t st, bool pdl) {
-  if (nblocks <= 0 || chunks <= 0) return cudaSuccess;
-  switch (P) {
-    case 1: return launch_predict_p<1>(ds, ch, map, nblocks, chunks, chain, mode, st, pdl);
-    case 2: return launch_predict_p<2>(ds, ch, map, nblocks, chunks, chain, mode, st, pdl);
-    case 3: return launch_predict_p<3>(ds, ch, map, nblocks, chunks, chain, mode, st, pdl);
-    case 4: return launch_predict_p<4>(ds, ch, map, nblocks, chunks, chain, mode, st, pdl);
-    case 5: return launch_predict_p<5>(ds, ch, map, nblocks, chunks, chain, mode, st, pdl);
-    case 6: return launch_predict_p<6>(ds, ch, map, nblocks, chunks, chain, mode, st, pdl);
-    case 7: return launch_predict_p<7>(ds, ch, map, nblocks, chunks, chain, mode, st, pdl);
-    case 8: return launch_predict_p<8>(ds, ch, map, nblocks, chunks, chain, mode, st, pdl);
-    default: return cudaErrorInvalidValue;
+// Dispatch on (P, S), 1 <= S <= P <= 8.
+template <template <int, int> class F, typename... A>
+auto dispatch_ps(int P, int S, A... a) -> decltype(F<1, 1>::f(a...)) {
+  switch (P * 16 + S) {
+#define BSG_C(P_, S_) \
+  case P_ * 16 + S_:  \
+    return F<P_, S_>::f(a...);
+    BSG_C(1, 1)
+    BSG_C(2, 1) BSG_C(2, 2)
+    BSG_C(3, 1) BSG_C(3, 2) BSG_C(3, 3)
+    BSG_C(4, 1) BSG_C(4, 2) BSG_C(4, 3) BSG_C(4, 4)
+    BSG_C(5, 1) BSG_C(5, 2) BSG_C(5, 3) BSG_C(5, 4) BSG_C(5, 5)
+    BSG_C(6, 1) BSG_C(6, 2) BSG_C(6, 3) BSG_C(6, 4) BSG_C(6, 5) BSG_C(6, 6)
+    BSG_C(7, 1) BSG_C(7, 2) BSG_C(7, 3) BSG_C(7, 4) BSG_C(7, 5) BSG_C(7, 6) BSG_C(7, 7)
+    BSG_C(8, 1) BSG_C(8, 2) BSG_C(8, 3) BSG_C(8, 4) BSG_C(8, 5) BSG_C(8, 6) BSG_C(8, 7)
+    BSG_C(8, 8)
+#undef BSG_C
+    default:
+      return F<1, 1>::fail();
   }
 }
 
+template <int P, int S>
+struct LaunchF {
+  static cudaError_t f(const DatasetDev *ds, ChainDev *ch, const BlockMap *map,
+                       int nblocks, int chunks, int chain, int mode, cudaStream_t st,
+                       bool pdl) {
+    return launch_predict_ps<P, S>(ds, ch, map, nblocks, chunks, chain, mode, st, pdl);
+  }
+  static cudaError_t fail() { return cudaErrorInvalidValue; }
+};
+
+template <int P, int S>
+struct OccF {
+  static int f(int) { return predict_blocks_per_sm_ps<P, S>(); }
+  static int fail() { return 1; }
+};
+
+}  // namespace
+
+cudaError_t launch_predict(int P, int S, const DatasetDev *ds, ChainDev *ch,
+                           const BlockMap *map, int nblocks, int chunks, int chain,
+                           int mode, cudaStream_t st, bool pdl) {
+  if (nblocks <= 0 || chunks <= 0) return cudaSuccess;
+  return dispatch_ps<LaunchF>(P, S, ds, ch, map, nblocks, chunks, chain, mode, st, pdl);
+}
+
+int predict_blocks_per_sm(int P, int S) { return dispatch_ps<OccF>(P, S, 0); }
 cudaError_t launch_predict_finish(const DatasetDev *ds, ChainDev *ch,
                                   const BlockMap *map, int nblocks, int chain,
                                   int mode, cudaStream_t st, bool pdl) {

@@ -20,13 +20,16 @@
 //                         array (covarGPU.cu:1106-1108) and advances the
 //                         host KISS stream once;
 //   compute_prbGPU        fills the reference's devicePrb and refreshes
-//                         deviceSpatCoef, which mcmc.cpp:606-607 copy back.
+//                         deviceSpatCoef, which mcmc.cpp:606-607 copy back;
+//   compute_predictGPU    runs the library's predictive pass on the current
+//                         coefficients and updates the host Qhat.
 // The Wishart degrees of freedom follow the reference GPU path,
 // df = TOTVOX + 19 (covarGPU.cu:1104).
 #include <cuda_runtime.h>
 #include <curand_kernel.h>
 
 #include <climits>
+#include <cmath>
 #include <cstdio>
 #include <vector>
 
@@ -49,7 +52,6 @@ struct ShimState {
   const unsigned char *data = nullptr;
   float beta = 0.f;
   bool failed = false;
-  bool warned_predict = false;
 };
 ShimState g;
 
@@ -156,16 +158,39 @@ void compute_prbGPU(float beta) {
                cudaMemcpyHostToDevice);
 }
 
-// The DIC / Qhat predictive pass (covarGPU.cu:1861-1957) is not part of the
-// sampler: it contributes 0 to ED and leaves Qhat unchanged.
-double compute_predictGPU(float, unsigned char *, unsigned char *, float *,
-                          float *, double **, int) {
-  if (!g.warned_predict) {
-    std::fprintf(stderr, "bsglmm_gb300 shim: compute_predictGPU (DIC/Qhat) is "
-                         "not provided; DIC.dat and Qhat*.dat are not computed\n");
-    g.warned_predict = true;
+// compute_predictGPU (covarGPU.cu:1866-1957): Mpredict [N][S] of the
+// current coefficients from the library's predictive pass; this subject's
+// own-group term is returned towards ED and Qhat is updated on the host as
+// the reference does (column 0 set on the first kept sweep, log-sums
+// otherwise).
+double compute_predictGPU(float beta, unsigned char *, unsigned char *,
+                          float *covar, float *, double **Qhat, int first) {
+  if (!g.ctx || NSUBTYPES < 1) return 0.0;
+  const int N = NSUBS, S = NSUBTYPES;
+  std::vector<double> mp((size_t)N * S);
+  report("bsg_set_beta_wm", bsg_set_beta_wm(g.ctx, g.ch, beta));
+  report("bsg_predict", bsg_predict(g.ctx, g.ch, mp.data()));
+  double dic = 0.0;
+  for (int i = 0; i < N; ++i) {
+    const double *m = &mp[(size_t)i * S];
+    int sub = 0;
+    for (int k = 0; k < S; ++k)
+      if (covar[(size_t)k * N + i] != 0.f) {
+        sub = k;
+        break;
+      }
+    dic += m[sub];
+    for (int k = 0; k < S; ++k) {
+      const double d = m[k] - m[sub];
+      if (first && k == 0) {
+        Qhat[i][0] = d;
+        continue;
+      }
+      const double mx = d > Qhat[i][k] ? d : Qhat[i][k];
+      Qhat[i][k] = std::log(std::exp(Qhat[i][k] - mx) + std::exp(d - mx)) + mx;
+    }
   }
-  return 0.0;
+  return dic;
 }
 
 // Paths the reference never takes with its shipped settings (probit

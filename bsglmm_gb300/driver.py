@@ -15,7 +15,9 @@ read_data.cpp:187-545, mcmc.cpp:795-964):
 * seed.dat: three integers (KISS state); rewritten at exit.
 * Outputs (FLOAT64 NIfTI-1, gzipped in process): empir_prb_<group>,
   total_lesion_cnt, total_empir_prb, spatCoef_<cov>, spatCoef_<cov>.Var,
-  standCoef_<cov>, prb_<group>.
+  standCoef_<cov>, prb_<group>; text: Qhat.dat, Qhat2.dat (mcmc.cpp:719-786)
+  and DIC.dat (mcmc.cpp:966-975), from the predictive pass that runs after
+  every kept sweep.
 
 The chain runs MaxIter+1 sweeps with the reference's burn-in and SAVE_ITER
 rule (mcmc.cpp:303-308) and the reference GPU path's Wishart df (V + 19,
@@ -156,6 +158,40 @@ def chain_key(seed):
     return ((hi << 32) ^ lo) & ((1 << 64) - 1)
 
 
+def qhat_lines(qhat, covar, ntypes, prior=None):
+    """Rows of Qhat.dat / Qhat2.dat (mcmc.cpp:719-786): subject, the
+    normalised exp(Qhat), the predicted group (last maximum) and the true
+    group (first nonzero group column, else 0).  With `prior`, Qhat is first
+    multiplied by it column-wise, as Qhat2.dat does."""
+    q = np.array(qhat, dtype=np.float64)
+    if prior is not None:
+        q = q * np.asarray(prior, dtype=np.float64)[None, :]
+    lines = []
+    for i in range(q.shape[0]):
+        mx = -np.finfo(np.float64).max
+        for g in range(ntypes):
+            mx = max(mx, q[i, g])
+        qh = np.log(np.sum(np.exp(q[i, :ntypes] - mx))) + mx
+        row = f"{i} " + "".join(f"{np.exp(q[i, g] - qh):.6f} " for g in range(ntypes))
+        mx, pred = -np.finfo(np.float64).max, -1
+        for g in range(ntypes):
+            if mx <= q[i, g]:
+                mx, pred = q[i, g], g
+        true = 0
+        for g in range(ntypes):
+            if covar[g, i] != 0:
+                true = g
+                break
+        lines.append(row + f"{pred} {true}\n")
+    return "".join(lines)
+
+
+def group_prior(covar, ntypes):
+    """grp_prior of read_data.cpp:287-316: the integer part of each group
+    column summed over subjects, divided by N."""
+    return np.trunc(covar[:ntypes].astype(np.float64)).sum(1) / covar.shape[1]
+
+
 def _print_state(it, omega, colmean, ntypes):
     """The periodic summary of mcmc.cpp:535-583."""
     V = np.linalg.inv(omega)
@@ -197,6 +233,8 @@ def run(ntypes, ncov, design, mask_name, maxiter, burnin, outdir=Path("."),
         ds = s.add_dataset(mask, covar, data, ntypes)
         ch = s.add_chain(ds, seed=key, burnin=burnin,
                          thin=save_iter_rule(maxiter, burnin), df_offset=19)
+        if ntypes >= 1:
+            s.set_predictive(ch, True)
         done = 0
         while done <= maxiter:
             step = min(PRINT_EVERY, maxiter + 1 - done)
@@ -206,16 +244,23 @@ def run(ntypes, ncov, design, mask_name, maxiter, burnin, outdir=Path("."),
             done += step
         maps = s.maps(ch)
         totsav = s.sweep_count(ch)[1]
+        qhat, _, npred = s.predictive(ch) if ntypes >= 1 else (None, 0.0, 0)
+        dic = s.dic(ch) if npred > 0 else dict.fromkeys(("DE", "ED", "PD", "DIC"), float("nan"))
     print(f"TOTSAV = {totsav}")
+    if qhat is not None:
+        (outdir / "Qhat.dat").write_text(qhat_lines(qhat, covar, ntypes))
+        (outdir / "Qhat2.dat").write_text(
+            qhat_lines(qhat, covar, ntypes, group_prior(covar, ntypes)))
     for p, nm in enumerate(names):
         nifti.write_nifti(outdir / f"spatCoef_{nm}.nii.gz", maps["spatCoef"][p], dims)
         nifti.write_nifti(outdir / f"spatCoef_{nm}.Var.nii.gz", maps["spatCoef.Var"][p], dims)
         nifti.write_nifti(outdir / f"standCoef_{nm}.nii.gz", maps["standCoef"][p], dims)
     for g in range(ntypes):
         nifti.write_nifti(outdir / f"prb_{names[g]}.nii.gz", maps["prb"][g], dims)
+    line = "DE = {DE:f} ED = {ED:f} PD = {PD:f} DIC = {DIC:f}".format(**dic)
+    print(line)
+    (outdir / "DIC.dat").write_text(line + "\n")
     Path("seed.dat").write_text(f"{seed[0]} {seed[1]} {seed[2]}\n")  # main.cu:430-432
-    print("DIC.dat and Qhat*.dat are not produced (the predictive pass is not part "
-          "of this sampler)")
     return maps, totsav
 
 

@@ -1,8 +1,9 @@
 // shim_harness.cpp -- test driver of covarGPU_shim.cu.  It plays the part of
 // the reference's main.cu / mcmc.cpp: defines their globals, fills them from
 // a study file and calls the launchers in the order of mcmc.cpp's GPU branch
-// (mcmc.cpp:318,356,367,605-607) for a number of sweeps, then writes the
-// resulting Omega, coefficients and lesion probabilities.
+// (mcmc.cpp:318,356,367,595,605-607) for a number of sweeps, keeping every
+// sweep after the first, then writes the resulting Omega, coefficients,
+// lesion probabilities, the ED sum and Qhat.
 //
 // usage: shim_harness <study.bin> <sweeps> <out.bin>
 #include <cuda_runtime.h>
@@ -37,6 +38,8 @@ void updateSpatCoefGPU(float *, float *, float *, float *, float *, float *,
                        float *, unsigned char *, float, float *, unsigned long *);
 void updateSpatCoefPrecGPU(float *, unsigned long *);
 void compute_prbGPU(float);
+double compute_predictGPU(float, unsigned char *, unsigned char *, float *,
+                          float *, double **, int);
 
 template <typename T>
 std::vector<T> rd(FILE *f, size_t n) {
@@ -74,12 +77,22 @@ int main(int argc, char **argv) {
   std::vector<float> spatCoef((size_t)NCOVAR * TOTVOXp, 0.f);
   const int sweeps = std::atoi(argv[2]);
   float beta = 0.f;
+  std::vector<double> qstore((size_t)NSUBS * (NSUBTYPES > 0 ? NSUBTYPES : 1), 0.0);
+  std::vector<double *> Qhat(NSUBS);  // mcmc.cpp:223-225
+  for (int i = 0; i < NSUBS; ++i) Qhat[i] = &qstore[(size_t)i * NSUBTYPES];
+  double ED = 0.0;
+  int totsav = 0;
   for (int iter = 0; iter < sweeps; ++iter) {
     updateZGPU(data.data(), beta, seed);
     updateSpatCoefGPU(covar.data(), spatCoef.data(), mean.data(), prec.data(),
                       nullptr, alphaMean.data(), nullptr, nullptr, beta,
                       wm.data(), seed);
     updateSpatCoefPrecGPU(prec.data(), seed);
+    if (iter > 0) {  // BURNIN = 0, SAVE_ITER = 1
+      ED += compute_predictGPU(beta, data.data(), nullptr, covar.data(), nullptr,
+                               Qhat.data(), totsav == 0);
+      ++totsav;
+    }
   }
   compute_prbGPU(beta);
   std::vector<float> prb((size_t)NSUBTYPES * TOTVOX);
@@ -93,6 +106,8 @@ int main(int argc, char **argv) {
   fwrite(alphaMean.data(), sizeof(float), alphaMean.size(), o);
   unsigned long long s3[3] = {seed[0], seed[1], seed[2]};
   fwrite(s3, 8, 3, o);
+  fwrite(&ED, sizeof(double), 1, o);
+  fwrite(qstore.data(), sizeof(double), qstore.size(), o);
   std::fclose(o);
   return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }

@@ -205,6 +205,23 @@ def test_empirical_maps_match_loop_restatement():
         cnt += int(flat[r])
 
 
+def test_qhat_lines_format_and_rules():
+    """Qhat.dat rows (mcmc.cpp:719-751): normalised exp(Qhat) with %.6f,
+    the predicted group is the last maximum, the true group the first
+    nonzero group column (else 0); Qhat2.dat scales by the group prior."""
+    q = np.array([[0.0, np.log(3.0)], [-1.0, -1.0], [2.0, -5.0]])
+    covar = np.array([[1, 0, 0], [0, 1, 0], [0.5, 0.2, 0.1]], np.float32)
+    text = driver.qhat_lines(q, covar, 2)
+    assert text.splitlines() == ["0 0.250000 0.750000 1 0",
+                                 "1 0.500000 0.500000 1 1",
+                                 "2 0.999089 0.000911 0 0"]
+    prior = driver.group_prior(np.array([[1.0, 1.0, 0.0], [0.0, 0.9, 1.0]]), 2)
+    assert np.allclose(prior, [2 / 3, 1 / 3])  # (int) of each entry
+    t2 = driver.qhat_lines(q, covar, 2, prior).splitlines()[0].split()
+    w = np.exp(q[0] * prior - np.logaddexp.reduce(q[0] * prior))
+    assert t2[1:3] == [f"{w[0]:.6f}", f"{w[1]:.6f}"]
+
+
 # ------------------------------------------------------------ seed stream --
 def test_kiss_matches_reference_stream(oracle_mod):
     seed = [123456789, 362436069, 521288629]
@@ -273,9 +290,20 @@ def test_driver_run_equals_native_chain(tmp_path, monkeypatch, capsys):
     with bsg.Sampler() as s:
         ds = s.add_dataset(st["mask"], st["covar"], st["data"], st["ntypes"])
         ch = s.add_chain(ds, seed=key, burnin=100, thin=1, df_offset=19)
+        s.set_predictive(ch, True)
         s.run(10101)
         maps = s.maps(ch)
         assert s.sweep_count(ch) == (10101, 10000)
+        qhat, ed, npred = s.predictive(ch)
+        dic = s.dic(ch)
+    assert npred == 10000
+    assert (tmp_path / "Qhat.dat").read_text() == driver.qhat_lines(
+        qhat, st["covar"], st["ntypes"])
+    assert (tmp_path / "Qhat2.dat").read_text() == driver.qhat_lines(
+        qhat, st["covar"], st["ntypes"], driver.group_prior(st["covar"], st["ntypes"]))
+    assert (tmp_path / "DIC.dat").read_text() == (
+        "DE = {DE:f} ED = {ED:f} PD = {PD:f} DIC = {DIC:f}\n".format(**dic))
+    assert dic["PD"] > 0
 
     def rd(name):
         return nifti.read_nifti(tmp_path / f"{name}.nii.gz").data

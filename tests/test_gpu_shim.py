@@ -72,14 +72,30 @@ def test_shim_reproduces_native_chain(tmp_path):
     hi = int(_kiss(ks) * 4294967296.0)
     lo = int(_kiss(ks) * 4294967296.0)
     key = ((hi << 32) ^ lo) & ((1 << 64) - 1)
+    o += 4 * P + 8 * 3  # column means, seed
+    ed_shim = np.frombuffer(raw, np.float64, 1, o)[0]; o += 8
+    q_shim = np.frombuffer(raw, np.float64, info["N"] * S, o).reshape(info["N"], S)
+    from oracle import qhat_update, subtypes
+    sub = subtypes(st.covar, S)
+    q = np.zeros((info["N"], S))
+    ed = 0.0
     with bsg.Sampler() as s:
         ds = s.add_dataset(st.mask, st.covar, st.data, 2)
         ch = s.add_chain(ds, seed=key, df_offset=19, burnin=2**31 - 1)
         om = np.eye(P, dtype=np.float32)
-        for _ in range(K):
+        for it in range(K):
             s.set_omega(ch, om.astype(np.float64))
             s.run(1)
             om = s.omega(ch).astype(np.float32)
+            if it > 0:
+                mp = s.predict(ch)
+                for i in range(info["N"]):
+                    ed += mp[i, sub[i]]
+                qhat_update(q, mp, sub, first=it == 1)
         assert np.array_equal(s.beta(ch), beta)
         assert np.array_equal(om, prec)
         assert np.allclose(s.compute_prb(ch), prb)
+    # compute_predictGPU through the shim = the library pass + the
+    # reference's host update of ED and Qhat
+    assert ed_shim == pytest.approx(ed, rel=1e-13)
+    assert np.allclose(q_shim, q, rtol=1e-12, atol=1e-12)

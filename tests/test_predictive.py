@@ -134,7 +134,7 @@ def test_qhat_update_restatement():
 
 # ------------------------------------------------------------------ GPU --
 @pytest.mark.gpu
-@pytest.mark.parametrize("P,S,wm", [(4, 2, True), (3, 1, False), (8, 3, False)])
+@pytest.mark.parametrize("P,S,wm", [(4, 2, True), (3, 1, False), (8, 3, False), (1, 1, False), (6, 6, True)])
 def test_gpu_predict_matches_oracle(oracle_mod, P, S, wm):
     import bsglmm_gb300 as bsg
     mask, covar, data, S, w = _indicator_study(20 + P, N=45, S=S, extra=P - S, wm=wm)

@@ -43,6 +43,7 @@ struct Chain {
 
 struct Group {
   int P = 0;
+  bool wm_any = false;  // a chain draws beta_WM: colour 0 waits for it
   std::vector<BlockMap> map[2];
   BlockMap *d_map[2] = {nullptr, nullptr};
   // predictive pass of the group's chains that have it on, one launch pair
@@ -55,6 +56,13 @@ struct Group {
     int pchunks = 0;
   };
   std::vector<Pred> pred;
+};
+
+// beta_WM of one chain on the device.
+struct WmState {
+  double sum;   // over kept sweeps
+  float beta;   // current value
+  int pad;
 };
 
 // Small per-chain counters of the predictive pass.
@@ -230,13 +238,13 @@ bsg_status ensure_partials(bsg_ctx *ctx, int vpb) {
     const size_t n1 = std::max<size_t>(1, (d.vox[1].size() + vpb - 1) / vpb);
     if (n0 > c.cap0) {
       dfree(ctx, c.dev.partials0);
-      c.dev.partials0 = (double *)dalloc(ctx, sizeof(double) * n0 * kMaxP, &e);
+      c.dev.partials0 = (double *)dalloc(ctx, sizeof(double) * n0 * kP0Vals, &e);
       CK(e);
       c.cap0 = n0;
     }
     if (n1 > c.cap1) {
       dfree(ctx, c.dev.partials1);
-      c.dev.partials1 = (double *)dalloc(ctx, sizeof(double) * n1 * kPostVals, &e);
+      c.dev.partials1 = (double *)dalloc(ctx, sizeof(double) * n1 * kFusedVals, &e);
       CK(e);
       c.cap1 = n1;
     }
@@ -299,6 +307,7 @@ bsg_status build_plan(bsg_ctx *ctx) {
       g->P = d.P;
     }
     for (int c = 0; c < 2; ++c) map_chain(g->map[c], (int)ci, (int)d.vox[c].size(), vpb, c);
+    if (ctx->ch[ci].dev.wm_update) g->wm_any = true;
     if (ctx->ch[ci].pred_on) {
       const ChainDev &cv = ctx->ch[ci].dev;
       Group::Pred *pr = nullptr;
@@ -345,8 +354,11 @@ cudaError_t enqueue_group(bsg_ctx *ctx, const Group &g, cudaStream_t st) {
   const Supplied sup{};
   cudaError_t e;
   for (int c = 0; c < 2; ++c) {
+    // the colour-0 latent phase reads beta_WM, which the previous colour-1
+    // kernel draws when the update is on: no early start then
+    const bool pdl = ctx->pdl && !(c == 0 && g.wm_any);
     e = launch_fused(g.P, ctx->lpv, ctx->threads, false, ctx->d_ds, ctx->d_ch,
-                     g.d_map[c], (int)g.map[c].size(), c, sup, st, ctx->pdl);
+                     g.d_map[c], (int)g.map[c].size(), c, sup, st, pdl);
     if (e != cudaSuccess) return e;
   }
   for (const auto &pr : g.pred) {
@@ -562,6 +574,67 @@ bsg_status bsg_add_dataset(bsg_ctx *ctx, const bsg_dataset_desc *desc,
     dv.wm = upload(ctx, q.wm, (size_t)d.V, &e);
     CK(e);
   }
+  // For the beta_WM update: column sums of X, c with X c = 1 (least
+  // squares, kept if the fit is exact to 1e-4: an intercept or group
+  // indicators that cover every subject), and sum_v WM_v^2.
+  {
+    const int P = d.P, N = d.N;
+    std::vector<double> A((size_t)P * P, 0.0), rhs(P, 0.0);
+    for (int i = 0; i < N; ++i)
+      for (int a = 0; a < P; ++a) {
+        const double xa = q.covar[(size_t)a * N + i];
+        rhs[a] += xa;
+        for (int b2 = 0; b2 < P; ++b2) A[a * P + b2] += xa * q.covar[(size_t)b2 * N + i];
+      }
+    std::vector<float> xsum(P), cvec(P, 0.f);
+    for (int a = 0; a < P; ++a) xsum[a] = (float)rhs[a];
+    std::vector<double> c = rhs;
+    bool ok = true;  // Gaussian elimination with partial pivoting
+    std::vector<double> M = A;
+    for (int k = 0; k < P && ok; ++k) {
+      int piv = k;
+      for (int r = k + 1; r < P; ++r)
+        if (std::fabs(M[r * P + k]) > std::fabs(M[piv * P + k])) piv = r;
+      if (!(std::fabs(M[piv * P + k]) > 1e-12 * (1.0 + std::fabs(A[k * P + k])))) {
+        ok = false;
+        break;
+      }
+      if (piv != k) {
+        for (int t = 0; t < P; ++t) std::swap(M[k * P + t], M[piv * P + t]);
+        std::swap(c[k], c[piv]);
+      }
+      for (int r = k + 1; r < P; ++r) {
+        const double f = M[r * P + k] / M[k * P + k];
+        for (int t = k; t < P; ++t) M[r * P + t] -= f * M[k * P + t];
+        c[r] -= f * c[k];
+      }
+    }
+    if (ok) {
+      for (int k = P - 1; k >= 0; --k) {
+        double t = c[k];
+        for (int u = k + 1; u < P; ++u) t -= M[k * P + u] * c[u];
+        c[k] = t / M[k * P + k];
+      }
+      for (int i = 0; i < N && ok; ++i) {
+        double f = 0.0;
+        for (int a = 0; a < P; ++a) f += c[a] * q.covar[(size_t)a * N + i];
+        ok = std::fabs(f - 1.0) < 1e-4;
+      }
+    }
+    dv.has_c = ok ? 1 : 0;
+    if (ok)
+      for (int a = 0; a < P; ++a) cvec[a] = (float)c[a];
+    dv.xsum = upload(ctx, xsum.data(), xsum.size(), &e);
+    CK(e);
+    dv.cvec = upload(ctx, cvec.data(), cvec.size(), &e);
+    CK(e);
+    double w2 = 0.0;
+    for (int v = 0; v < d.V; ++v) {
+      const double w = q.wm ? (double)q.wm[v] : 1.0;
+      w2 += w * w;
+    }
+    dv.wm2 = w2;
+  }
   uint8_t *bytes = upload(ctx, q.data, (size_t)d.N * d.V, &e);
   CK(e);
   int *status = (int *)dalloc(ctx, sizeof(int), &e);
@@ -630,7 +703,7 @@ bsg_status bsg_add_chain(bsg_ctx *ctx, int32_t dataset_id,
   cv.key0 = (uint32_t)(desc->seed & 0xFFFFFFFFu);
   cv.key1 = (uint32_t)(desc->seed >> 32);
   cv.chain_id = (uint32_t)ctx->ch.size();
-  cv.beta_wm = desc->beta_wm;
+  cv.wm_update = 0;
   cv.df_offset = desc->df_offset;
   cv.burnin = desc->burnin;
   cv.thin = desc->thin;
@@ -647,6 +720,12 @@ bsg_status bsg_add_chain(bsg_ctx *ctx, int32_t dataset_id,
   CK(e);
   cv.colmean = (float *)dalloc(ctx, sizeof(float) * P, &e);
   CK(e);
+  WmState *wst = (WmState *)dalloc(ctx, sizeof(WmState), &e);
+  CK(e);
+  const WmState w0{0.0, desc->beta_wm, 0};
+  CK(cudaMemcpy(wst, &w0, sizeof(w0), cudaMemcpyHostToDevice));
+  cv.wm_sum = &wst->sum;
+  cv.wm_beta = &wst->beta;
   CK(cudaMemset(cv.colmean, 0, sizeof(float) * P));
   const size_t nacc = (size_t)P * d.V, nprb = (size_t)d.S * d.V;
   cv.acc_sum = (double *)dalloc(ctx, sizeof(double) * nacc, &e);
@@ -898,14 +977,44 @@ bsg_status bsg_set_omega(bsg_ctx *ctx, int32_t chain, const double *in) {
 bsg_status bsg_set_beta_wm(bsg_ctx *ctx, int32_t chain, float beta_wm) {
   if (!valid_chain(ctx, chain) || !std::isfinite(beta_wm)) return BSG_ERR_INVALID;
   Chain &c = ctx->ch[chain];
-  c.dev.beta_wm = beta_wm;
   c.desc.beta_wm = beta_wm;
-  if (ctx->plan_valid) {  // graphs read the descriptor from device memory
-    CK(cudaSetDevice(ctx->device));
-    CK(cudaMemcpyAsync(&ctx->d_ch[chain].beta_wm, &c.dev.beta_wm, sizeof(float),
-                       cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
-  }
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaMemcpyAsync(c.dev.wm_beta, &beta_wm, sizeof(float), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return BSG_OK;
+}
+
+bsg_status bsg_set_wm_update(bsg_ctx *ctx, int32_t chain, int32_t enable) {
+  if (!valid_chain(ctx, chain)) return BSG_ERR_INVALID;
+  Chain &c = ctx->ch[chain];
+  const Dataset &d = ctx->ds[c.dataset];
+  if (enable && !d.dev.has_c)
+    return fail(ctx, BSG_ERR_UNSUPPORTED,
+                "the beta_WM update needs design columns that sum to 1 for every "
+                "subject (an intercept or a full set of group indicators)");
+  if (enable && !(d.dev.wm2 > 0.0))
+    return fail(ctx, BSG_ERR_INVALID, "the beta_WM update needs a nonzero WM map");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const int32_t on = enable ? 1 : 0;
+  if (c.dev.wm_update != on) ctx->plan_valid = false;
+  c.dev.wm_update = on;
+  return BSG_OK;
+}
+
+bsg_status bsg_get_beta_wm(bsg_ctx *ctx, int32_t chain, float *beta_wm,
+                           double *mean_kept) {
+  if (!valid_chain(ctx, chain)) return BSG_ERR_INVALID;
+  const Chain &c = ctx->ch[chain];
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  WmState w{};
+  CK(cudaMemcpy(&w, c.dev.wm_sum, sizeof(w), cudaMemcpyDeviceToHost));
+  long long nk = 0;
+  CK(cudaMemcpy(&nk, c.dev.nkept, sizeof(nk), cudaMemcpyDeviceToHost));
+  if (beta_wm) *beta_wm = w.beta;
+  if (mean_kept) *mean_kept = nk > 0 ? w.sum / (double)nk : 0.0;
   return BSG_OK;
 }
 
@@ -1023,6 +1132,7 @@ bsg_status bsg_reset_accumulators(bsg_ctx *ctx, int32_t chain) {
   CK(cudaMemset(c.dev.acc_sq, 0, sizeof(double) * n));
   if (d.S) CK(cudaMemset(c.dev.prb_sum, 0, sizeof(double) * (size_t)d.S * d.V));
   CK(cudaMemset(c.dev.nkept, 0, sizeof(long long)));
+  CK(cudaMemset(c.dev.wm_sum, 0, sizeof(double)));
   if (c.dev.pred_part) {
     CK(cudaMemset(c.dev.qhat, 0, sizeof(double) * (size_t)d.N * std::max(d.S, 1)));
     CK(cudaMemset(c.dev.pred_sums, 0, sizeof(double) * 2));
@@ -1046,6 +1156,10 @@ struct PredCkpt {
   long long npred;
   double ed_sum;
 };
+struct WmCkpt {  // beta_WM state; the header holds the current value
+  int32_t update, pad;
+  double sum;
+};
 
 size_t ckpt_bytes_v1(const Dataset &d) {
   return sizeof(CkptHeader) + sizeof(float) * (size_t)d.P * d.Vp +
@@ -1055,7 +1169,7 @@ size_t ckpt_bytes_v1(const Dataset &d) {
 
 size_t ckpt_bytes(const Dataset &d) {
   return ckpt_bytes_v1(d) + sizeof(PredCkpt) +
-         sizeof(double) * (size_t)d.N * std::max(d.S, 1);
+         sizeof(double) * (size_t)d.N * std::max(d.S, 1) + sizeof(WmCkpt);
 }
 }  // namespace
 
@@ -1072,8 +1186,10 @@ bsg_status bsg_checkpoint(bsg_ctx *ctx, int32_t chain, void *buf, int64_t size) 
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   char *p = static_cast<char *>(buf);
+  WmState ws{};
+  CK(cudaMemcpy(&ws, c.dev.wm_sum, sizeof(ws), cudaMemcpyDeviceToHost));
   CkptHeader h{kCkptMagic, 2, d.P, d.Vp, d.V, d.S, c.dev.df_offset, c.dev.burnin,
-               c.dev.thin, c.dev.key0, c.dev.key1, c.dev.chain_id, c.dev.beta_wm};
+               c.dev.thin, c.dev.key0, c.dev.key1, c.dev.chain_id, ws.beta};
   std::memcpy(p, &h, sizeof(h));
   p += sizeof(h);
   auto get = [&](const void *src, size_t n) -> cudaError_t {
@@ -1097,8 +1213,12 @@ bsg_status bsg_checkpoint(bsg_ctx *ctx, int32_t chain, void *buf, int64_t size) 
   p += sizeof(pk);
   if (c.dev.pred_part)
     CK(get(c.dev.qhat, sizeof(double) * nq));
-  else
+  else {
     std::memset(p, 0, sizeof(double) * nq);
+    p += sizeof(double) * nq;
+  }
+  const WmCkpt wk{c.dev.wm_update, 0, ws.sum};
+  std::memcpy(p, &wk, sizeof(wk));
   return BSG_OK;
 }
 
@@ -1151,13 +1271,27 @@ bsg_status bsg_restore(bsg_ctx *ctx, int32_t chain, const void *buf, int64_t siz
     CK(cudaMemcpy(c.dev.pred_sums, sums, sizeof(sums), cudaMemcpyHostToDevice));
   }
   c.pred_on = pk.on != 0;
+  WmCkpt wk{0, 0, 0.0};
+  if (h.version == 2) {
+    p = static_cast<const char *>(buf) + ckpt_bytes(d) - sizeof(WmCkpt);
+    std::memcpy(&wk, p, sizeof(wk));
+  } else {
+    long long nk = 0;  // v1: beta_WM was fixed, so its kept sum is nk beta_WM
+    CK(cudaMemcpy(&nk, c.dev.nkept, sizeof(nk), cudaMemcpyDeviceToHost));
+    wk.sum = (double)nk * (double)h.beta_wm;
+  }
+  if (wk.update && !d.dev.has_c)
+    return fail(ctx, BSG_ERR_UNSUPPORTED, "checkpoint has the beta_WM update on");
+  const WmState ws{wk.sum, h.beta_wm, 0};
+  CK(cudaMemcpy(c.dev.wm_sum, &ws, sizeof(ws), cudaMemcpyHostToDevice));
+  c.dev.wm_update = wk.update;
+  c.desc.beta_wm = h.beta_wm;
   c.dev.df_offset = h.df_offset;
   c.dev.burnin = h.burnin;
   c.dev.thin = h.thin;
   c.dev.key0 = h.key0;
   c.dev.key1 = h.key1;
   c.dev.chain_id = h.chain_id;
-  c.dev.beta_wm = h.beta_wm;
   ctx->plan_valid = false;  // descriptors changed
   return BSG_OK;
 }
@@ -1209,6 +1343,9 @@ bsg_status bsg_sweep_supplied(bsg_ctx *ctx, int32_t chain, const uint32_t *ubits
   if (s) return s;
   const Chain &c = ctx->ch[chain];
   const Dataset &d = ctx->ds[c.dataset];
+  if (c.dev.wm_update)
+    return fail(ctx, BSG_ERR_UNSUPPORTED,
+                "supplied-variate sweeps take beta_WM as given (turn its update off)");
   cudaError_t e;
   const int P = d.P, nw = P * (P - 1) / 2;
   Supplied sup{};

@@ -65,11 +65,14 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
 
   float beta[P], acc[P];
   int v = 0, sc = 0;
-  float bwm = 0.f;
+  float bwm = 0.f, wmv = 0.f;
   if (active) {
     sc = d.nb[colour][j];
     v = d.vidx[colour][j];
-    bwm = ch.beta_wm * (d.wm ? d.wm[v] : 1.f);
+    wmv = d.wm ? d.wm[v] : 1.f;
+    // beta_WM is final since the previous colour-1 launch: with its update
+    // on, colour-0 launches do not start early (no programmatic launch)
+    bwm = *ch.wm_beta * wmv;
 #pragma unroll
     for (int p = 0; p < P; ++p) beta[p] = ch.beta[(size_t)p * Vp + sc];
   } else {
@@ -195,6 +198,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
   int err = ok ? 0 : kErrTnCap;
   float bnew[P];   // the voxel's coefficients at the end of the sweep
   float pv[NT];    // its Omega pair products (colour 1)
+  double wmt = 0.0;  // its term of the beta_WM conditional mean
 #pragma unroll
   for (int p = 0; p < P; ++p) bnew[p] = beta[p];
 #pragma unroll
@@ -293,6 +297,19 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
     }
     err |= (okc ? 0 : kErrChol) | ((okc && !fin) ? kErrNaN : 0);
 
+    // ---- beta_WM | Z, beta (betaMGPU, covarGPU.cu:585-640): this voxel's
+    // WM_v * sum_i (Z_iv - x_i' beta_v) with the new beta_v; with X c = 1,
+    // sum_i (Z_iv - bwm) = c' acc.
+    if (ch.wm_update) {
+      double sz = 0.0, sxb = 0.0;
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        sz += (double)d.cvec[p] * (double)acc[p];
+        sxb += (double)d.xsum[p] * (double)bnew[p];
+      }
+      wmt = (double)wmv * (sz + (double)d.N * (double)bwm - sxb);
+    }
+
     // ---- posterior running sums of the kept sweep (mcmc.cpp:637-645) --
     if (kept) {
 #pragma unroll
@@ -344,28 +361,31 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
     atomicOr(ch.any_status, err);
   }
 
-  // ---- block partials: column sums (both colours) and pairs (colour 1) --
-  __shared__ double red[kMaxThreads / 32][kPostVals];
-  __shared__ double tot[kPostVals];
+  // ---- block partials: column sums and the beta_WM term (both colours),
+  // pairs (colour 1)
+  __shared__ double red[kMaxThreads / 32][kFusedVals];
+  __shared__ double tot[kFusedVals];
   __shared__ int is_last;
   const int lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
   constexpr int kColOff = kMaxPairs;
 #pragma unroll
-  for (int q = 0; q < NT + P; ++q) {
+  for (int q = 0; q <= NT + P; ++q) {
     if (colour == 0 && q < NT) continue;
-    double val = q < NT ? (double)pv[q] : (double)bnew[q - NT];
+    double val = q < NT ? (double)pv[q] : (q < NT + P ? (double)bnew[q - NT] : wmt);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
-    if (lane == 0) red[warp][q < NT ? q : kColOff + (q - NT)] = val;
+    if (lane == 0)
+      red[warp][q < NT ? q : (q < NT + P ? kColOff + (q - NT) : kWmOff)] = val;
   }
   __syncthreads();
   const int vpb = blockDim.x / LPV;
   const int lb = bm.start / vpb;
   if (colour == 0) {
-    if (tid < P) {
+    if (tid < P || tid == kMaxP) {
+      const int q = tid < P ? kColOff + tid : kWmOff;
       double s = 0.0;
-      for (int w = 0; w < nwarp; ++w) s += red[w][kColOff + tid];
-      ch.partials0[(size_t)lb * kMaxP + tid] = s;
+      for (int w = 0; w < nwarp; ++w) s += red[w][q];
+      ch.partials0[(size_t)lb * kP0Vals + tid] = s;
       __threadfence();
     }
     __syncthreads();
@@ -379,12 +399,13 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
     }
     return;
   }
-  if (tid < kPostVals) {
-    const bool live = tid < kMaxPairs ? tid < NT : (tid - kColOff) < P;
+  if (tid < kFusedVals) {
+    const bool live =
+        tid < kMaxPairs ? tid < NT : (tid == kWmOff || (tid - kColOff) < P);
     double s = 0.0;
     if (live)
       for (int w = 0; w < nwarp; ++w) s += red[w][tid];
-    ch.partials1[(size_t)lb * kPostVals + tid] = s;
+    ch.partials1[(size_t)lb * kFusedVals + tid] = s;
     __threadfence();
   }
   __syncthreads();
@@ -400,15 +421,17 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
   // reproducible): warp w takes values q = w, w + nwarp, ...
   const int n0 = d.n[0];
   const int nblk0 = (n0 + vpb - 1) / vpb;
-  for (int q = warp; q < kPostVals; q += nwarp) {
-    const bool live = q < kMaxPairs ? q < NT : (q - kColOff) < P;
+  for (int q = warp; q < kFusedVals; q += nwarp) {
+    const bool live = q < kMaxPairs ? q < NT : (q == kWmOff || (q - kColOff) < P);
     double s = 0.0;
     if (live) {
       for (int bb = lane; bb < nblk1; bb += 32)
-        s += __ldcg(ch.partials1 + (size_t)bb * kPostVals + q);
-      if (q >= kColOff)
+        s += __ldcg(ch.partials1 + (size_t)bb * kFusedVals + q);
+      if (q >= kColOff) {
+        const int q0 = q == kWmOff ? kMaxP : q - kColOff;
         for (int bb = lane; bb < nblk0; bb += 32)
-          s += __ldcg(ch.partials0 + (size_t)bb * kMaxP + (q - kColOff));
+          s += __ldcg(ch.partials0 + (size_t)bb * kP0Vals + q0);
+      }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);

@@ -11,6 +11,11 @@ namespace bsg {
 constexpr int kMaxP = 8;                            // covariates per chain
 constexpr int kMaxPairs = kMaxP * (kMaxP + 1) / 2;  // lower-triangle pairs
 constexpr int kPostVals = kMaxPairs + kMaxP;        // pairs + column sums
+// Partial rows of the colour kernels: colour 0 holds the column sums and the
+// beta_WM term, colour 1 the pairs, the column sums and the beta_WM term.
+constexpr int kP0Vals = kMaxP + 1;
+constexpr int kFusedVals = kPostVals + 1;
+constexpr int kWmOff = kPostVals;                    // beta_WM term's slot
 constexpr int kChunk = 512;                         // subjects staged per pass
 constexpr int kChunkPad = kChunk + kChunk / 32;     // one pad word per 32
 constexpr float kATail = 5.0f;  // inversion below, rejection above
@@ -34,6 +39,7 @@ enum : uint32_t {
   kTagBeta = 3,
   kTagWNorm = 4,
   kTagGamma = 5,
+  kTagWm = 6,
 };
 
 // Sticky per-chain error bits (ChainDev::status).
@@ -53,6 +59,10 @@ struct DatasetDev {
   const float *covar;          // [P][N]
   const float *xtx;            // [P][P]  X'X in float (read_data.cpp:321)
   const float *wm;             // [V] or nullptr (WM = 1)
+  const float *xsum;           // [P] sum over subjects of each design column
+  const float *cvec;           // [P] c with X c = 1 (all subjects), if has_c
+  int32_t has_c;               // the design spans the constant
+  double wm2;                  // sum over in-mask voxels of WM_v^2
   const int32_t *nb[2];        // [7][n_c]: sc(self), sc of the 6 neighbours
                                // in the order -x, +x, -y, +y, -z, +z
   const uint8_t *nbm[2];       // [n_c] bit t set iff neighbour t is in mask
@@ -64,7 +74,9 @@ struct DatasetDev {
 struct ChainDev {
   int32_t dataset;
   uint32_t key0, key1, chain_id;
-  float beta_wm;
+  float *wm_beta;          // [1] beta_WM, the white-matter coefficient
+  double *wm_sum;          // [1] sum of beta_WM over kept sweeps
+  int32_t wm_update;       // draw beta_WM | Z, beta every sweep
   int32_t df_offset, burnin, thin;
   float *beta;             // [P][Vp]
   float *omega_f;          // [P*P] float copy read by the colour kernels
@@ -73,8 +85,9 @@ struct ChainDev {
   double *acc_sum;         // [P][V]  sum of beta over kept sweeps
   double *acc_sq;          // [P][V]  sum of beta^2
   double *prb_sum;         // [S][V]  sum of the lesion probability
-  double *partials0;       // [colour-0 blocks][kMaxP] column sums
-  double *partials1;       // [colour-1 blocks][kPostVals] pairs + column sums
+  double *partials0;       // [colour-0 blocks][kP0Vals] column sums, WM term
+  double *partials1;       // [colour-1 blocks][kFusedVals] pairs, column sums,
+                           // WM term
   unsigned int *done;      // [2] arrival counters of the colour kernels
   long long *sweep;        // [2] sweeps completed by the colour-c kernel;
                            // sweep[1] is the chain's completed-sweep count

@@ -59,7 +59,7 @@ __global__ void prb_kernel(const DatasetDev *__restrict__ dsv,
     const int c = pos < n0 ? 0 : 1;
     const int j = c ? pos - n0 : pos;
     const int sc = d.nb[c][j], v = d.vidx[c][j];
-    const float bwm = ch.beta_wm * (d.wm ? d.wm[v] : 1.f);
+    const float bwm = *ch.wm_beta * (d.wm ? d.wm[v] : 1.f);
     for (int g = 0; g < d.S; ++g)
       prb[(size_t)g * d.V + v] = prob_sdnorm(ch.beta[(size_t)g * d.Vp + sc] + bwm);
   }

@@ -99,6 +99,8 @@ __global__ void __launch_bounds__(kPredThreads)
 #pragma unroll
   for (int g = 0; g < S; ++g) acc[g] = 0.0;
   const double inv_nk = de ? 1.0 / (double)(*ch.nkept > 0 ? *ch.nkept : 1) : 0.0;
+  // beta_WM: the current value, or its mean over kept sweeps for DE (MWM)
+  const float bwc = de ? (float)(*ch.wm_sum * inv_nk) : *ch.wm_beta;
 
   const int t0 = tile * tw, t1 = min(t0 + tw, ntot);
   for (int q0 = t0; q0 < t1; q0 += kPredSub) {
@@ -117,7 +119,7 @@ __global__ void __launch_bounds__(kPredThreads)
         else
           b[p] = 0.f;
       }
-      b[P] = ch.beta_wm * (d.wm ? d.wm[v] : 1.f);
+      b[P] = bwc * (d.wm ? d.wm[v] : 1.f);
 #pragma unroll
       for (int u = 0; u < Q; ++u)
         Bs[tid][u] = make_float4(b[4 * u], b[4 * u + 1], b[4 * u + 2], b[4 * u + 3]);

@@ -62,6 +62,7 @@ static __device__ void wishart_warp(const ChainDev &ch, const DatasetDev &d,
   __shared__ double A[kMaxP][kMaxP], Ai[kMaxP][kMaxP], T[kMaxP][kMaxP],
       B[kMaxP][kMaxP];
   const int P = d.P;
+  const uint32_t cid = ch.chain_id << 8, sw = (uint32_t)sweep;
   int err = 0;
   if (lane < P)
     for (int c = 0; c < P; ++c) {
@@ -93,7 +94,6 @@ static __device__ void wishart_warp(const ChainDev &ch, const DatasetDev &d,
   }
   if (ok) {
     const double df = (double)d.V + (double)ch.df_offset;
-    const uint32_t cid = ch.chain_id << 8, sw = (uint32_t)sweep;
     if (lane < P) {
       const double c2 = supplied ? sup.chi2[lane]
                                  : 2.0 * gamma_mt(0.5 * (df - lane), (uint32_t)lane,
@@ -153,6 +153,24 @@ static __device__ void wishart_warp(const ChainDev &ch, const DatasetDev &d,
     err |= kErrWishart;
   }
   if (lane < P) ch.colmean[lane] = (float)(tot[kMaxPairs + lane] / (double)d.V);
+  if (lane == 0) {
+    // beta_WM | Z, beta ~ N(var * sum_v WM_v sum_i (Z_iv - x_i' beta_v),
+    // var = 1 / (N sum_v WM_v^2)) (updateBetaGPU, covarGPU.cu:680-720)
+    float bw = *ch.wm_beta;
+    if (ch.wm_update && !supplied) {
+      const double var = 1.0 / ((double)d.N * d.wm2);
+      const uint4 r = philox1(make_uint4(0u, 0u, sw, cid | kTagWm), ch.key0, ch.key1);
+      const double z = (double)normal_of(pick4(r, 0));
+      const float nb = (float)(var * tot[kWmOff] + sqrt(var) * z);
+      if (isfinite(nb)) {
+        bw = nb;
+        *ch.wm_beta = nb;
+      } else {
+        err |= kErrNaN;
+      }
+    }
+    if (kept) *ch.wm_sum += (double)bw;  // MWM of mcmc.cpp:636
+  }
   err = __reduce_or_sync(0xffffffffu, err);
   if (lane == 0) {
     if (err) {

@@ -22,7 +22,9 @@
 //   compute_prbGPU        fills the reference's devicePrb and refreshes
 //                         deviceSpatCoef, which mcmc.cpp:606-607 copy back;
 //   compute_predictGPU    runs the library's predictive pass on the current
-//                         coefficients and updates the host Qhat.
+//                         coefficients and updates the host Qhat;
+//   updateBetaGPU         turns on the library's beta_WM draw (at the end of
+//                         each sweep) and returns the latest beta_WM.
 // The Wishart degrees of freedom follow the reference GPU path,
 // df = TOTVOX + 19 (covarGPU.cu:1104).
 #include <cuda_runtime.h>
@@ -52,6 +54,8 @@ struct ShimState {
   const unsigned char *data = nullptr;
   float beta = 0.f;
   bool failed = false;
+  bool wm_update = false;  // updateBetaGPU has been called
+  bool wm_on = false;      // the chain draws beta_WM
 };
 ShimState g;
 
@@ -122,11 +126,17 @@ void updateSpatCoefGPU(float *covar, float *, float *, float *SpatCoefPrec,
                        float beta, float *WM, unsigned long *seed) {
   g.beta = beta;
   if (!ensure(covar, WM, seed)) return;
+  if (g.wm_update && !g.wm_on) {
+    report("bsg_set_wm_update", bsg_set_wm_update(g.ctx, g.ch, 1));
+    g.wm_on = true;
+  }
   const int P = NCOVAR;
   std::vector<double> om((size_t)P * P);
   for (int i = 0; i < P * P; ++i) om[i] = (double)SpatCoefPrec[i];
   report("bsg_set_omega", bsg_set_omega(g.ctx, g.ch, om.data()));
-  report("bsg_set_beta_wm", bsg_set_beta_wm(g.ctx, g.ch, beta));
+  // with the beta_WM update on, the device value (drawn at the end of each
+  // sweep) is the chain's; the host copy is one draw behind
+  if (!g.wm_on) report("bsg_set_beta_wm", bsg_set_beta_wm(g.ctx, g.ch, beta));
   report("bsg_run", bsg_run(g.ctx, 1));
   report("bsg_sync", bsg_sync(g.ctx));
   std::vector<float> cm(P);
@@ -145,7 +155,7 @@ void updateSpatCoefPrecGPU(float *SpatCoefPrec, unsigned long *seed) {
 
 void compute_prbGPU(float beta) {
   if (!g.ctx) return;
-  report("bsg_set_beta_wm", bsg_set_beta_wm(g.ctx, g.ch, beta));
+  if (!g.wm_on) report("bsg_set_beta_wm", bsg_set_beta_wm(g.ctx, g.ch, beta));
   std::vector<float> prb((size_t)NSUBTYPES * TOTVOX + 1);
   std::vector<float> b((size_t)NCOVAR * TOTVOXp);
   report("bsg_compute_prb", bsg_compute_prb(g.ctx, g.ch, prb.data()));
@@ -168,7 +178,7 @@ double compute_predictGPU(float beta, unsigned char *, unsigned char *,
   if (!g.ctx || NSUBTYPES < 1) return 0.0;
   const int N = NSUBS, S = NSUBTYPES;
   std::vector<double> mp((size_t)N * S);
-  report("bsg_set_beta_wm", bsg_set_beta_wm(g.ctx, g.ch, beta));
+  if (!g.wm_on) report("bsg_set_beta_wm", bsg_set_beta_wm(g.ctx, g.ch, beta));
   report("bsg_predict", bsg_predict(g.ctx, g.ch, mp.data()));
   double dic = 0.0;
   for (int i = 0; i < N; ++i) {
@@ -193,14 +203,23 @@ double compute_predictGPU(float beta, unsigned char *, unsigned char *,
   return dic;
 }
 
-// Paths the reference never takes with its shipped settings (probit
-// MODEL = 1, NCOV_FIX = 0, WM argument 0): defined so the program links,
-// they report that they are unsupported.
-void updateBetaGPU(float *, float *, float *, float *, float *, float, float,
+// updateBetaGPU (covarGPU.cu:686-724; mcmc.cpp:344-345 with the WM
+// argument): the library draws beta_WM | Z, beta at the end of every sweep,
+// after both colours' coefficients (Z_0, beta_0, Z_1, beta_1, beta_WM,
+// Omega).  This call switches that update on for the next sweep and
+// returns the beta_WM drawn by the previous one.
+void updateBetaGPU(float *beta, float *, float *, float *, float *, float, float,
                    float *, float *, unsigned long *) {
-  std::fprintf(stderr, "bsglmm_gb300 shim: the WM coefficient update "
-                       "(updateBetaGPU) is not supported; beta_WM stays fixed\n");
+  g.wm_update = true;
+  if (!g.ctx || !g.wm_on) return;
+  float b = *beta;
+  report("bsg_get_beta_wm", bsg_get_beta_wm(g.ctx, g.ch, &b, nullptr));
+  *beta = b;
 }
+
+// Paths the reference never takes with its shipped settings (probit
+// MODEL = 1, NCOV_FIX = 0): defined so the program links, they report that
+// they are unsupported.
 void updatePhiGPU(float, float *) {
   std::fprintf(stderr, "bsglmm_gb300 shim: MODEL != 1 is not supported\n");
 }

@@ -12,17 +12,19 @@ read_data.cpp:187-545, mcmc.cpp:795-964):
   subject: id, NCov covariates, lesion-map file name relative to ./images.
   The first NTypes covariates are the group columns.
 * Lesion maps: FLOAT32 or FLOAT64 NIfTI-1, binary.
+* WM: "0" for none, "1" for images/avg152T1_white.nii.gz, else a UINT8
+  NIfTI-1 image in ./images; WM_v = value / 255 (read_data.cpp:489-545) and
+  the white-matter coefficient beta_WM is drawn every sweep.
 * seed.dat: three integers (KISS state); rewritten at exit.
 * Outputs (FLOAT64 NIfTI-1, gzipped in process): empir_prb_<group>,
   total_lesion_cnt, total_empir_prb, spatCoef_<cov>, spatCoef_<cov>.Var,
   standCoef_<cov>, prb_<group>; text: Qhat.dat, Qhat2.dat (mcmc.cpp:719-786)
   and DIC.dat (mcmc.cpp:966-975), from the predictive pass that runs after
-  every kept sweep.
+  every kept sweep; bWM (mcmc.cpp:830-837) with a WM image.
 
 The chain runs MaxIter+1 sweeps with the reference's burn-in and SAVE_ITER
 rule (mcmc.cpp:303-308) and the reference GPU path's Wishart df (V + 19,
-covarGPU.cu:1104).  WM = "0" only: the white-matter coefficient update is
-not part of this sampler; GPU = 1 only.
+covarGPU.cu:1104).  GPU = 1 only.
 """
 from __future__ import annotations
 
@@ -46,7 +48,7 @@ USAGE = """Usage: bsglmm  NTypes  NCov  GPU  Design Mask WM [MaxIter BurnIn]
   GPU     - 1 use GPU (this build has no CPU path)
   Design  - Text file, tab or space separated data file
   Mask    - Filename of mask image in './images' directory, or '1' to use default (mask.nii.gz)
-  WM      - '0' (the white-matter covariate update is not provided)
+  WM      - Filename of WM image in './images' directory, '0' to use none, or '1' to use default (avg152T1_white.nii.gz)
   MaxIter - Number of iterations (defaults to 100,000)
   BurnIn  - Number of burn-in iterations (defaults to 50,000)"""
 
@@ -67,6 +69,18 @@ def read_mask(path: Path) -> np.ndarray:
         raise DriverError(f"Incorrect data type in file: {img.datatype}\n"
                           "Must be float (NIFTI_TYPE_FLOAT64)")
     return (_as_byte(img.data) != 0).astype(np.uint8)
+
+
+def read_wm(path: Path, mask: np.ndarray) -> np.ndarray:
+    """read_nifti1_WM (read_data.cpp:489-545): a UINT8 image; WM_v = value /
+    255 over in-mask voxels in file order."""
+    img = nifti.read_nifti(path)
+    if img.datatype != nifti.UINT8:
+        raise DriverError(f"Incorrect data type in file: {img.datatype}\n"
+                          "Must be unsigned char (NIFTI_TYPE_UINT8)")
+    if img.data.shape != mask.shape:
+        raise DriverError(f"{path}: dimensions {img.dims} differ from the mask's")
+    return (img.data[mask.astype(bool)].astype(np.float32) / np.float32(255.0))
 
 
 def read_design(path: Path, ncov: int, ntypes: int):
@@ -210,9 +224,10 @@ def _print_state(it, omega, colmean, ntypes):
 
 
 def run(ntypes, ncov, design, mask_name, maxiter, burnin, outdir=Path("."),
-        device=0, quiet=False):
+        device=0, quiet=False, wm_name=None):
     outdir = Path(outdir)
     mask = read_mask(IMAGE_DIR / mask_name)
+    wm = read_wm(IMAGE_DIR / wm_name, mask) if wm_name else None
     names, covar, images = read_design(design, ncov, ntypes)
     if ntypes > ncov:
         raise DriverError("NTypes cannot exceed NCov")
@@ -230,9 +245,11 @@ def run(ntypes, ncov, design, mask_name, maxiter, burnin, outdir=Path("."),
     seed = read_seed(Path("seed.dat"))
     key = chain_key(seed)
     with Sampler(device) as s:
-        ds = s.add_dataset(mask, covar, data, ntypes)
+        ds = s.add_dataset(mask, covar, data, ntypes, wm)
         ch = s.add_chain(ds, seed=key, burnin=burnin,
                          thin=save_iter_rule(maxiter, burnin), df_offset=19)
+        if wm is not None:
+            s.set_wm_update(ch, True)
         if ntypes >= 1:
             s.set_predictive(ch, True)
         done = 0
@@ -245,6 +262,7 @@ def run(ntypes, ncov, design, mask_name, maxiter, burnin, outdir=Path("."),
         maps = s.maps(ch)
         totsav = s.sweep_count(ch)[1]
         qhat, _, npred = s.predictive(ch) if ntypes >= 1 else (None, 0.0, 0)
+        bwm_mean = s.beta_wm(ch)[1]
         dic = s.dic(ch) if npred > 0 else dict.fromkeys(("DE", "ED", "PD", "DIC"), float("nan"))
     print(f"TOTSAV = {totsav}")
     if qhat is not None:
@@ -257,6 +275,10 @@ def run(ntypes, ncov, design, mask_name, maxiter, burnin, outdir=Path("."),
         nifti.write_nifti(outdir / f"standCoef_{nm}.nii.gz", maps["standCoef"][p], dims)
     for g in range(ntypes):
         nifti.write_nifti(outdir / f"prb_{names[g]}.nii.gz", maps["prb"][g], dims)
+    if wm is not None:  # mean over kept sweeps of beta_WM WM_v (mcmc.cpp:636,799)
+        bwm = np.zeros(mask.shape)
+        bwm[mask.astype(bool)] = bwm_mean * wm.astype(np.float64)
+        nifti.write_nifti(outdir / "bWM.nii.gz", bwm, dims)
     line = "DE = {DE:f} ED = {ED:f} PD = {PD:f} DIC = {DIC:f}".format(**dic)
     print(line)
     (outdir / "DIC.dat").write_text(line + "\n")
@@ -285,11 +307,9 @@ def main(argv=None) -> int:
     try:
         if gpu != 1:
             raise DriverError("GPU = 0 (the reference's untested CPU path) is not provided")
-        if wm_arg != "0":
-            raise DriverError("WM covariate: only '0' is supported (the WM coefficient "
-                              "update is not part of this sampler)")
         mask_name = DEFAULT_MASK if mask_arg == "1" else mask_arg
-        run(ntypes, ncov, design, mask_name, maxiter, burnin)
+        wm_name = None if wm_arg == "0" else (DEFAULT_WM if wm_arg == "1" else wm_arg)
+        run(ntypes, ncov, design, mask_name, maxiter, burnin, wm_name=wm_name)
     except (DriverError, nifti.NiftiError) as e:
         print(f"Error: {e}", file=sys.stderr)
         return 2

@@ -231,6 +231,19 @@ class Sampler:
         self._check(self._L.bsg_reset_accumulators(self._h, chain),
                     "bsg_reset_accumulators")
 
+    # ------------------------------------------------ beta_WM update --
+    def set_wm_update(self, chain: int = 0, enable: bool = True):
+        """Draw beta_WM | Z, beta every sweep (updateBetaGPU)."""
+        self._check(self._L.bsg_set_wm_update(self._h, chain, int(bool(enable))),
+                    "bsg_set_wm_update")
+
+    def beta_wm(self, chain: int = 0):
+        """(current beta_WM, its mean over kept sweeps)."""
+        b, m = C.c_float(), C.c_double()
+        self._check(self._L.bsg_get_beta_wm(self._h, chain, C.byref(b), C.byref(m)),
+                    "bsg_get_beta_wm")
+        return b.value, m.value
+
     # ------------------------------------------------- DIC / Qhat pass --
     def set_predictive(self, chain: int = 0, enable: bool = True):
         """Run the DIC / Qhat pass (compute_predictGPU) after every kept

@@ -123,9 +123,21 @@ bsg_status bsg_get_beta(bsg_ctx *ctx, int32_t chain, float *spatcoef);
 bsg_status bsg_set_beta(bsg_ctx *ctx, int32_t chain, const float *spatcoef);
 bsg_status bsg_get_omega(bsg_ctx *ctx, int32_t chain, double *omega);
 bsg_status bsg_set_omega(bsg_ctx *ctx, int32_t chain, const double *omega);
-/* Sets the fixed white-matter coefficient beta_WM of a chain (the value the
- * reference's updateBetaGPU draws, covarGPU.cu:686-724). */
+/* Sets the white-matter coefficient beta_WM of a chain (eta gains
+ * beta_WM WM_v, covarGPU.cu:1386); fixed unless its update is on. */
 bsg_status bsg_set_beta_wm(bsg_ctx *ctx, int32_t chain, float beta_wm);
+/* The beta_WM update (updateBetaGPU, covarGPU.cu:686-724, called by
+ * mcmc.cpp:344-345 when the WM argument is given): each sweep draws
+ * beta_WM ~ N(var sum_v WM_v sum_i (Z_iv - x_i' beta_v), var), var = 1 /
+ * (N sum_v WM_v^2), after both colours' coefficient updates (the sweep is
+ * Z_0, beta_0, Z_1, beta_1, beta_WM, Omega).  Needs design columns that sum
+ * to 1 for every subject (BSG_ERR_UNSUPPORTED otherwise) and a nonzero WM.
+ * Off by default; kept in checkpoints. */
+bsg_status bsg_set_wm_update(bsg_ctx *ctx, int32_t chain, int32_t enable);
+/* Current beta_WM and its mean over kept sweeps (the bWM map of
+ * mcmc.cpp:795-840 is that mean times WM_v).  Either pointer may be NULL. */
+bsg_status bsg_get_beta_wm(bsg_ctx *ctx, int32_t chain, float *beta_wm,
+                           double *mean_kept);
 /* Column means of the last sweep (covarGPU.cu:563-583). */
 bsg_status bsg_get_colmeans(bsg_ctx *ctx, int32_t chain, float *means);
 bsg_status bsg_get_sweep(bsg_ctx *ctx, int32_t chain, int64_t *sweep,

@@ -657,17 +657,23 @@ static int chain_wishart(const orc_problem *pb, const orc_chain_cfg *cfg,
 int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
                   int64_t nsweeps, double *spatcoef, double *omega,
                   double *acc_sum, double *acc_sq, double *prb_sum,
-                  int64_t *nkept) {
+                  int64_t *nkept, double *beta_wm, double *wm_sum) {
   int N = pb->N, P = pb->P, V = pb->V, Vp = pb->Vp, S = pb->S, err = 0;
   uint32_t k0 = cfg->key0, k1 = cfg->key1, ch = cfg->chain;
   double *prb = (double *)malloc(sizeof(double) * ((size_t)S * V + 1));
+  double bw = beta_wm ? *beta_wm : cfg->beta_wm;
+  double xsum[16] = {0}, wm2 = 0.0;
+  for (int p = 0; p < P; ++p)
+    for (int i = 0; i < N; ++i) xsum[p] += pb->covar[p * N + i];
+  for (int v = 0; v < V; ++v) wm2 += (double)pb->wm[v] * pb->wm[v];
   for (int64_t s = s0; s < s0 + nsweeps; ++s) {
     uint32_t sw = (uint32_t)s;
+    double wmr = 0.0; /* sum_v WM_v sum_i (Z_iv - x_i' beta_v), new beta */
     for (int c = 0; c < 2; ++c)
       for (int j = 0; j < pb->n[c]; ++j) {
         int vox = pb->vox[c][j], v = pb->idx[vox], sc = pb->idxsc[vox];
-        double bwm = cfg->beta_wm * pb->wm[v];
-        double b[16] = {0}, e[16];
+        double bwm = bw * pb->wm[v];
+        double b[16] = {0}, e[16], zs = 0.0;
         uint32_t o[4];
         for (int i = 0; i < N; ++i) {
           if ((i & 3) == 0)
@@ -689,6 +695,7 @@ int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
               err |= ORC_ERR_TN_CAP;
           }
           double z = y ? mu + t : mu - t;
+          zs += z;
           for (int p = 0; p < P; ++p) b[p] += pb->covar[p * N + i] * (z - bwm);
         }
         for (int p = 0; p < P; p += 4) {
@@ -699,11 +706,25 @@ int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
         }
         if (!beta_voxel(pb, c, j, b, omega, e, 1, spatcoef))
           err |= ORC_ERR_CHOL;
+        double xb = 0.0;
+        for (int p = 0; p < P; ++p) xb += xsum[p] * spatcoef[(size_t)p * Vp + sc];
+        wmr += pb->wm[v] * (zs - xb);
       }
+    /* beta_WM | Z, beta (updateBetaGPU, covarGPU.cu:680-720): normal with
+     * variance 1 / (N sum WM^2) and mean variance * wmr; the lesion
+     * probabilities of this sweep use the beta_WM of its latent draws. */
+    double bw_used = bw;
+    if (cfg->wm_update) {
+      uint32_t o[4];
+      philox(0u, 0u, sw, (ch << 8) | ORC_TAG_WM, k0, k1, o);
+      double var = 1.0 / ((double)N * wm2);
+      bw = (double)(float)(var * wmr + sqrt(var) * orc_normal_from_bits(o[0]));
+    }
     err |= chain_wishart(pb, cfg, sw, spatcoef, omega);
     int kept = (s > cfg->burnin) && (s % (cfg->thin > 0 ? cfg->thin : 1) == 0);
+    if (kept && wm_sum) *wm_sum += bw;
     if (kept && acc_sum) { /* running sums of mcmc.cpp:637-645 */
-      orc_compute_prb(pb, cfg->beta_wm, spatcoef, prb);
+      orc_compute_prb(pb, bw_used, spatcoef, prb);
       ++(*nkept);
       for (int p = 0; p < pb->nsize; ++p) {
         if (!pb->msk[p]) continue;
@@ -718,6 +739,7 @@ int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
     }
   }
   free(prb);
+  if (beta_wm) *beta_wm = bw;
   return err;
 }
 

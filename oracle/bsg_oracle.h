@@ -108,18 +108,21 @@ typedef struct {
   uint32_t chain;         /* chain id, part of every counter */
   int32_t df_offset;      /* Wishart df = V + df_offset */
   int32_t burnin, thin;   /* kept iff sweep > burnin && sweep % thin == 0 */
-  double beta_wm;
+  double beta_wm;         /* initial beta_WM */
+  int32_t wm_update;      /* draw beta_WM | Z, beta after both colours */
 } orc_chain_cfg;
 
-/* Runs sweeps [s0, s0 + nsweeps) from state (spatcoef, omega) in FP64 using
- * the same counter layout as the GPU sampler.  Accumulates (if acc_sum !=
+/* Runs sweeps [s0, s0 + nsweeps) from state (spatcoef, omega, *beta_wm) in
+ * FP64 using the same counter layout and scan as the GPU sampler: per
+ * colour Z_v then beta_v, then (wm_update) beta_WM | Z, beta, then Omega.
+ * beta_wm may be NULL (cfg->beta_wm, fixed).  Accumulates (if acc_sum !=
  * NULL) the running sums acc_sum[P][V], acc_sq[P][V], prb_sum[S][V] of
- * mcmc.cpp:637-645 and *nkept.
- * Returns an OR of error flags (0 = ok). */
+ * mcmc.cpp:637-645, *wm_sum (if not NULL, the kept beta_WM values) and
+ * *nkept.  Returns an OR of error flags (0 = ok). */
 int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
                   int64_t nsweeps, double *spatcoef, double *omega,
                   double *acc_sum, double *acc_sq, double *prb_sum,
-                  int64_t *nkept);
+                  int64_t *nkept, double *beta_wm, double *wm_sum);
 
 /* ------------------------------- CPU timing port of the reference sweep -- */
 /* A reentrant restatement of the reference's CPU sweep (mcmc.cpp:395-434:
@@ -146,6 +149,7 @@ int64_t orc_port_updates(const orc_port *pt, int nvox_limit);
 #define ORC_TAG_BETA 3u
 #define ORC_TAG_WNORM 4u
 #define ORC_TAG_GAMMA 5u
+#define ORC_TAG_WM 6u
 
 #define ORC_A_TAIL 5.0      /* inversion below, Robert rejection above */
 #define ORC_TAIL_MAX 16     /* rejection attempts per draw */

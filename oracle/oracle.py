@@ -74,7 +74,7 @@ def lib() -> C.CDLL:
             "orc_loglik_as": (_d, [_d, _i]),
             "orc_predict": (None, [_P, _d, _P, _P]),
             "orc_dic_de": (_d, [_P, _P, _P]),
-            "orc_chain_run": (_i, [_P, _P, _i64, _i64, _P, _P, _P, _P, _P, _P]),
+            "orc_chain_run": (_i, [_P, _P, _i64, _i64, _P, _P, _P, _P, _P, _P, _P, _P]),
             "orc_port_new": (_P, [_P, C.c_uint64, _i]),
             "orc_port_free": (None, [_P]),
             "orc_port_sweep": (None, [_P, _i]),
@@ -91,7 +91,7 @@ def lib() -> C.CDLL:
 class ChainCfg(C.Structure):
     _fields_ = [("key0", C.c_uint32), ("key1", C.c_uint32), ("chain", C.c_uint32),
                 ("df_offset", C.c_int32), ("burnin", C.c_int32), ("thin", C.c_int32),
-                ("beta_wm", C.c_double)]
+                ("beta_wm", C.c_double), ("wm_update", C.c_int32)]
 
 
 def philox(ctr, key) -> np.ndarray:
@@ -216,10 +216,14 @@ class Problem:
 
     def chain(self, seed: int, nsweeps: int, chain_id: int = 0, burnin: int = 0,
               thin: int = 1, df_offset=None, beta_wm=0.0, s0: int = 0,
-              spatcoef=None, omega=None):
+              spatcoef=None, omega=None, wm_update: bool = False):
+        """FP64 chain on the sampler's counters.  Returns the state (beta,
+        omega, beta_wm) and the posterior summaries of the kept sweeps."""
         cfg = ChainCfg(seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF, chain_id,
                        self.P if df_offset is None else df_offset, burnin, thin,
-                       beta_wm)
+                       beta_wm, int(bool(wm_update)))
+        bw = C.c_double(beta_wm)
+        wsum = C.c_double(0.0)
         b = (np.zeros((self.P, self.Vp)) if spatcoef is None
              else np.array(spatcoef, dtype=np.float64, order="C"))
         om = np.eye(self.P) if omega is None else np.array(omega, dtype=np.float64, order="C")
@@ -228,14 +232,17 @@ class Problem:
         sp = np.zeros((max(self.S, 1), self.V))
         nk = C.c_int64(0)
         err = self._L.orc_chain_run(self.h, C.byref(cfg), s0, nsweeps, _p(b), _p(om),
-                                    _p(s1), _p(s2), _p(sp), C.byref(nk))
+                                    _p(s1), _p(s2), _p(sp), C.byref(nk), C.byref(bw),
+                                    C.byref(wsum))
         T = nk.value
         with np.errstate(invalid="ignore", divide="ignore"):
             mean = s1 / T
             var = (s2 - T * mean * mean) / (T - 1)
             prb = sp[: self.S] / T
+            wm_mean = wsum.value / T if T else float("nan")
         return dict(beta=b, omega=om, mean=mean, var=var, prb=prb,
-                    sum=s1, sumsq=s2, nkept=T, err=err)
+                    sum=s1, sumsq=s2, nkept=T, err=err, beta_wm=bw.value,
+                    wm_sum=wsum.value, wm_mean=wm_mean)
 
 
 def subtypes(covar, S: int) -> np.ndarray:

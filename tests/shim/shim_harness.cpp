@@ -5,7 +5,9 @@
 // sweep after the first, then writes the resulting Omega, coefficients,
 // lesion probabilities, the ED sum and Qhat.
 //
-// usage: shim_harness <study.bin> <sweeps> <out.bin>
+// usage: shim_harness <study.bin> <sweeps> <out.bin> [wm]
+// With "wm" the study file also holds V floats of WM after the seed and the
+// harness calls updateBetaGPU before each coefficient update (UPDATE_WM).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -37,6 +39,8 @@ void updateZGPU(unsigned char *, float, unsigned long *);
 void updateSpatCoefGPU(float *, float *, float *, float *, float *, float *,
                        float *, unsigned char *, float, float *, unsigned long *);
 void updateSpatCoefPrecGPU(float *, unsigned long *);
+void updateBetaGPU(float *, float *, float *, float *, float *, float, float,
+                   float *, float *, unsigned long *);
 void compute_prbGPU(float);
 double compute_predictGPU(float, unsigned char *, unsigned char *, float *,
                           float *, double **, int);
@@ -52,7 +56,8 @@ std::vector<T> rd(FILE *f, size_t n) {
 }
 
 int main(int argc, char **argv) {
-  if (argc != 4) return 2;
+  if (argc != 4 && argc != 5) return 2;
+  UPDATE_WM = argc == 5;
   FILE *f = std::fopen(argv[1], "rb");
   if (!f) return 2;
   auto hdr = rd<int32_t>(f, 8);
@@ -63,9 +68,10 @@ int main(int argc, char **argv) {
   auto covar = rd<float>(f, (size_t)NCOVAR * NSUBS);
   auto data = rd<uint8_t>(f, (size_t)NSUBS * TOTVOX);
   auto seed0 = rd<uint64_t>(f, 3);
+  std::vector<float> wm(TOTVOX, 1.0f);
+  if (UPDATE_WM) wm = rd<float>(f, TOTVOX);
   std::fclose(f);
   hostIdx = idx.data();
-  std::vector<float> wm(TOTVOX, 1.0f);
   unsigned long seed[3] = {(unsigned long)seed0[0], (unsigned long)seed0[1],
                            (unsigned long)seed0[2]};
   cudaMalloc(&deviceSpatCoef, sizeof(float) * (size_t)NCOVAR * TOTVOXp);
@@ -84,6 +90,9 @@ int main(int argc, char **argv) {
   int totsav = 0;
   for (int iter = 0; iter < sweeps; ++iter) {
     updateZGPU(data.data(), beta, seed);
+    if (UPDATE_WM)  // mcmc.cpp:344-345
+      updateBetaGPU(&beta, nullptr, nullptr, nullptr, nullptr, 0.f, 1e-6f, nullptr,
+                    nullptr, seed);
     updateSpatCoefGPU(covar.data(), spatCoef.data(), mean.data(), prec.data(),
                       nullptr, alphaMean.data(), nullptr, nullptr, beta,
                       wm.data(), seed);
@@ -94,6 +103,9 @@ int main(int argc, char **argv) {
       ++totsav;
     }
   }
+  if (UPDATE_WM)  // the beta_WM the next iteration would start from
+    updateBetaGPU(&beta, nullptr, nullptr, nullptr, nullptr, 0.f, 1e-6f, nullptr,
+                  nullptr, seed);
   compute_prbGPU(beta);
   std::vector<float> prb((size_t)NSUBTYPES * TOTVOX);
   cudaMemcpy(spatCoef.data(), deviceSpatCoef, sizeof(float) * spatCoef.size(),
@@ -108,6 +120,7 @@ int main(int argc, char **argv) {
   fwrite(s3, 8, 3, o);
   fwrite(&ED, sizeof(double), 1, o);
   fwrite(qstore.data(), sizeof(double), qstore.size(), o);
+  fwrite(&beta, sizeof(float), 1, o);
   std::fclose(o);
   return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }

@@ -146,6 +146,19 @@ def test_read_design_and_lesions(tmp_path, monkeypatch):
     assert np.array_equal(data, st["data"])
 
 
+def test_read_wm(tmp_path):
+    mask = np.zeros((2, 3, 4), np.uint8)
+    mask[0, 1, :3] = mask[1, 2, 1] = 1
+    vol = np.arange(24, dtype=np.float64).reshape(2, 3, 4) * 10
+    nifti.write_nifti(tmp_path / "wm.nii.gz", vol, (4, 3, 2), datatype=nifti.UINT8)
+    wm = driver.read_wm(tmp_path / "wm.nii.gz", mask)
+    assert wm.dtype == np.float32
+    assert np.array_equal(wm, vol[mask.astype(bool)].astype(np.float32) / np.float32(255))
+    nifti.write_nifti(tmp_path / "wm64.nii", vol, (4, 3, 2))
+    with pytest.raises(driver.DriverError, match="UINT8"):
+        driver.read_wm(tmp_path / "wm64.nii", mask)
+
+
 def test_mask_byte_conversion():
     """(unsigned char) of the mask's doubles: truncation, then the low byte."""
     v = np.array([0.0, 0.99, 1.0, 1.7, 255.9, 256.0, 257.5])
@@ -262,7 +275,7 @@ def test_cli_usage_and_unsupported_options(tmp_path, monkeypatch, capsys):
     assert driver.main(["1", "2", "0", "d.txt", "1", "0"]) == 2
     assert "GPU = 0" in capsys.readouterr().err
     assert driver.main(["1", "2", "1", "d.txt", "1", "1"]) == 2
-    assert "WM" in capsys.readouterr().err
+    assert "mask.nii.gz: no such file" in capsys.readouterr().err
     assert driver.main(["1", "2", "1", "d.txt", "1", "0", "10", "20"]) == 2
     out = capsys.readouterr()
     assert "Silly-small" in out.out and "Burn-in exceeds" in out.out
@@ -346,3 +359,36 @@ def test_driver_short_run_matches_oracle_chain(tmp_path, monkeypatch, oracle_mod
     for g in range(st["ntypes"]):
         got = nifti.read_nifti(tmp_path / f"prb_{st['names'][g]}.nii.gz").data[m]
         assert np.allclose(got, o["prb"][g], rtol=1e-4, atol=1e-4)
+
+
+@pytest.mark.gpu
+def test_driver_wm_run_equals_native_chain(tmp_path, monkeypatch):
+    """With a WM image the run draws beta_WM every sweep and writes bWM, the
+    kept-sweep mean of beta_WM WM_v; the maps equal the native chain's."""
+    import bsglmm_gb300 as bsg
+    monkeypatch.chdir(tmp_path)
+    st = write_study(tmp_path, seed=13, N=26)
+    X, Y, Z = st["dims"]
+    rng = np.random.default_rng(14)
+    wmvol = rng.integers(0, 256, (Z, Y, X)).astype(np.float64)
+    nifti.write_nifti(tmp_path / "images" / "wm.nii.gz", wmvol, (X, Y, Z),
+                      datatype=nifti.UINT8)
+    assert driver.main([str(st["ntypes"]), str(st["P"]), "1", "design.txt", "1",
+                        "wm.nii.gz", "300", "100"]) == 0
+    m = st["mask"].astype(bool)
+    wm = (wmvol[m].astype(np.float32) / np.float32(255))
+    key = driver.chain_key([1, 2, 2])
+    with bsg.Sampler() as s:
+        ds = s.add_dataset(st["mask"], st["covar"], st["data"], st["ntypes"], wm)
+        ch = s.add_chain(ds, seed=key, burnin=100, thin=200, df_offset=19)
+        s.set_wm_update(ch, True)
+        s.set_predictive(ch, True)
+        s.run(301)
+        maps = s.maps(ch)
+        cur, mean = s.beta_wm(ch)
+    for p, nm in enumerate(st["names"]):
+        got = nifti.read_nifti(tmp_path / f"spatCoef_{nm}.nii.gz").data
+        assert np.array_equal(got, maps["spatCoef"][p])
+    bwm = nifti.read_nifti(tmp_path / "bWM.nii.gz").data
+    assert np.array_equal(bwm[m], mean * wm.astype(np.float64))
+    assert np.all(bwm[~m] == 0) and mean != 0.0

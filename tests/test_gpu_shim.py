@@ -99,3 +99,55 @@ def test_shim_reproduces_native_chain(tmp_path):
     # reference's host update of ED and Qhat
     assert ed_shim == pytest.approx(ed, rel=1e-13)
     assert np.allclose(q_shim, q, rtol=1e-12, atol=1e-12)
+
+
+def test_shim_wm_update_reproduces_native_chain(tmp_path):
+    """With the WM argument (UPDATE_WM) the harness calls updateBetaGPU
+    before every coefficient update, as mcmc.cpp:344-345 does; the shimmed
+    program equals the native chain with its beta_WM update on."""
+    import bsglmm_gb300 as bsg
+    from bsglmm_gb300 import synth
+    st = synth.small_study(73, shape=(10, 9, 8), N=48, P=3, S=1)
+    wm = np.random.default_rng(74).random(st.V).astype(np.float32)
+    seed0 = [2468, 1357, 9753]
+    with bsg.Sampler() as s:
+        ds = s.add_dataset(st.mask, st.covar, st.data, 1, wm)
+        info = s.info(ds)
+        lat = s.lattice(ds)
+    hdr = np.array([info["X"], info["Y"], info["Z"], info["N"], info["P"], info["S"],
+                    info["V"], info["Vp"]], np.int32)
+    study = tmp_path / "study.bin"
+    with open(study, "wb") as f:
+        for a in (hdr, lat["idx"].astype(np.int32), st.covar.astype(np.float32),
+                  st.data.astype(np.uint8), np.array(seed0, np.uint64), wm):
+            f.write(np.ascontiguousarray(a).tobytes())
+    exe = _build(tmp_path)
+    K = 5
+    out = tmp_path / "out.bin"
+    r = subprocess.run([str(exe), str(study), str(K), str(out), "wm"],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    P, Vp, V, S, N = info["P"], info["Vp"], info["V"], info["S"], info["N"]
+    raw = out.read_bytes()
+    o = 0
+    prec = np.frombuffer(raw, np.float32, P * P, o).reshape(P, P); o += 4 * P * P
+    beta = np.frombuffer(raw, np.float32, P * Vp, o).reshape(P, Vp); o += 4 * P * Vp
+    o += 4 * S * V + 4 * P + 8 * 3 + 8 + 8 * N * S  # prb, means, seed, ED, Qhat
+    bwm_shim = np.frombuffer(raw, np.float32, 1, o)[0]
+    ks = list(seed0)
+    hi = int(_kiss(ks) * 4294967296.0)
+    lo = int(_kiss(ks) * 4294967296.0)
+    key = ((hi << 32) ^ lo) & ((1 << 64) - 1)
+    with bsg.Sampler() as s:
+        ds = s.add_dataset(st.mask, st.covar, st.data, 1, wm)
+        ch = s.add_chain(ds, seed=key, df_offset=19, burnin=2**31 - 1)
+        s.set_wm_update(ch, True)
+        om = np.eye(P, dtype=np.float32)
+        for _ in range(K):
+            s.set_omega(ch, om.astype(np.float64))
+            s.run(1)
+            om = s.omega(ch).astype(np.float32)
+        assert np.array_equal(s.beta(ch), beta)
+        assert np.array_equal(om, prec)
+        b_native, _ = s.beta_wm(ch)
+    assert bwm_shim == b_native and bwm_shim != 0.0

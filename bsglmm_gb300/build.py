@@ -27,6 +27,7 @@ SOURCES = [
     "bsg_fused_l2.cu",
     "bsg_fused_l4.cu",
     "bsg_fused_l8.cu",
+    "bsg_fused_mix.cu",
     "bsg_kernels.cu",
     "bsg_peak.cu",
     "bsg_noalloc.cu",

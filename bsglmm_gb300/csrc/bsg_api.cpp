@@ -43,6 +43,7 @@ struct Chain {
 
 struct Group {
   int P = 0;
+  bool mix = false;     // t/logit chains (scale-mixture colour kernel)
   bool wm_any = false;  // a chain draws beta_WM: colour 0 waits for it
   std::vector<BlockMap> map[2];
   BlockMap *d_map[2] = {nullptr, nullptr};
@@ -298,15 +299,19 @@ bsg_status build_plan(bsg_ctx *ctx) {
   ctx->groups.clear();
   for (size_t ci = 0; ci < ctx->ch.size(); ++ci) {
     const Dataset &d = ctx->ds[ctx->ch[ci].dataset];
+    const bool mix = ctx->ch[ci].dev.model != 1;
     Group *g = nullptr;
     for (auto &gg : ctx->groups)
-      if (gg.P == d.P) g = &gg;
+      if (gg.P == d.P && gg.mix == mix) g = &gg;
     if (!g) {
       ctx->groups.push_back(Group());
       g = &ctx->groups.back();
       g->P = d.P;
+      g->mix = mix;
     }
-    for (int c = 0; c < 2; ++c) map_chain(g->map[c], (int)ci, (int)d.vox[c].size(), vpb, c);
+    // the t/logit kernel runs one lane per voxel
+    const int gvpb = mix ? ctx->threads : vpb;
+    for (int c = 0; c < 2; ++c) map_chain(g->map[c], (int)ci, (int)d.vox[c].size(), gvpb, c);
     if (ctx->ch[ci].dev.wm_update) g->wm_any = true;
     if (ctx->ch[ci].pred_on) {
       const ChainDev &cv = ctx->ch[ci].dev;
@@ -350,15 +355,23 @@ bsg_status build_plan(bsg_ctx *ctx) {
 // Enqueues one sweep of every chain: per P group the two colour kernels
 // (groups on parallel branches when there are several); the colour-1
 // kernel also reduces the Omega pairs and draws Omega.
-cudaError_t enqueue_group(bsg_ctx *ctx, const Group &g, cudaStream_t st) {
+// One colour kernel of a group.
+cudaError_t launch_colour(bsg_ctx *ctx, const Group &g, int c, cudaStream_t st, bool pdl) {
+  if (g.mix)
+    return launch_fused_mix(g.P, ctx->threads, ctx->d_ds, ctx->d_ch, g.d_map[c],
+                            (int)g.map[c].size(), c, st, pdl);
   const Supplied sup{};
+  return launch_fused(g.P, ctx->lpv, ctx->threads, false, ctx->d_ds, ctx->d_ch,
+                      g.d_map[c], (int)g.map[c].size(), c, sup, st, pdl);
+}
+
+cudaError_t enqueue_group(bsg_ctx *ctx, const Group &g, cudaStream_t st) {
   cudaError_t e;
   for (int c = 0; c < 2; ++c) {
     // the colour-0 latent phase reads beta_WM, which the previous colour-1
     // kernel draws when the update is on: no early start then
     const bool pdl = ctx->pdl && !(c == 0 && g.wm_any);
-    e = launch_fused(g.P, ctx->lpv, ctx->threads, false, ctx->d_ds, ctx->d_ch,
-                     g.d_map[c], (int)g.map[c].size(), c, sup, st, pdl);
+    e = launch_colour(ctx, g, c, st, pdl);
     if (e != cudaSuccess) return e;
   }
   for (const auto &pr : g.pred) {
@@ -470,6 +483,33 @@ bsg_status ensure_pred(bsg_ctx *ctx, Chain &c) {
   cv.pred_tile = tile;
   cv.pred_part = part;
   ctx->plan_valid = false;  // the device copy of the chain changed
+  return BSG_OK;
+}
+
+// Link of a chain (the reference's MODEL and its t_df / logit_factor,
+// main.cu:42,168-175).  The t/logit links start from weights phi = 1.
+bsg_status set_model(bsg_ctx *ctx, Chain &c, int model) {
+  const Dataset &d = ctx->ds[c.dataset];
+  ChainDev &cv = c.dev;
+  cudaError_t e;
+  if (model != 1) {
+    for (int k = 0; k < 2; ++k) {
+      const size_t n = (size_t)d.N * d.vox[k].size();
+      if (!cv.phi[k]) {
+        cv.phi[k] = (float *)dalloc(ctx, sizeof(float) * (n ? n : 1), &e);
+        CK(e);
+      }
+      CK(launch_fill(cv.phi[k], n, 1.0f, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  cv.model = model;
+  cv.t_df = model == 0 ? 8.f : (model == 2 ? 3.f : 1000.f);
+  cv.inv_lf = model == 0 ? (float)(1.0 / 0.634) : 1.f;
+  const double alpha = 0.5 * ((double)cv.t_df + 1.0), dd = alpha - 1.0 / 3.0;
+  cv.mix_d = (float)dd;
+  cv.mix_c = (float)(1.0 / std::sqrt(9.0 * dd));
+  ctx->plan_valid = false;
   return BSG_OK;
 }
 
@@ -704,6 +744,9 @@ bsg_status bsg_add_chain(bsg_ctx *ctx, int32_t dataset_id,
   cv.key1 = (uint32_t)(desc->seed >> 32);
   cv.chain_id = (uint32_t)ctx->ch.size();
   cv.wm_update = 0;
+  cv.model = 1;  // probit (main.cu:42)
+  cv.t_df = 1000.f;
+  cv.inv_lf = 1.f;
   cv.df_offset = desc->df_offset;
   cv.burnin = desc->burnin;
   cv.thin = desc->thin;
@@ -852,14 +895,12 @@ bsg_status bsg_profile(bsg_ctx *ctx, int64_t nsweeps, double *ms,
   if (s) return s;
   std::vector<cudaEvent_t> ev((size_t)3 * nsweeps);
   for (auto &e : ev) CK(cudaEventCreate(&e));
-  const Supplied sup{};
   int64_t nl[3] = {0, 0, 0};
   for (int64_t i = 0; i < nsweeps; ++i) {
     for (int c = 0; c < 2; ++c) {
       CK(cudaEventRecord(ev[3 * i + c], ctx->stream));
       for (const Group &g : ctx->groups) {
-        CK(launch_fused(g.P, ctx->lpv, ctx->threads, false, ctx->d_ds, ctx->d_ch,
-                        g.d_map[c], (int)g.map[c].size(), c, sup, ctx->stream));
+        CK(launch_colour(ctx, g, c, ctx->stream, false));
         nl[c]++;
       }
     }
@@ -890,7 +931,7 @@ int64_t bsg_launches_per_sweep(const bsg_ctx *ctx) {
   std::vector<int> ps, pp;
   for (auto &c : ctx->ch) {
     const Dataset &d = ctx->ds[c.dataset];
-    const int P = d.P, PS = d.P * 16 + d.S;
+    const int P = d.P * 2 + (c.dev.model != 1), PS = d.P * 16 + d.S;
     if (std::find(ps.begin(), ps.end(), P) == ps.end()) ps.push_back(P);
     if (c.pred_on && std::find(pp.begin(), pp.end(), PS) == pp.end()) pp.push_back(PS);
   }
@@ -995,6 +1036,8 @@ bsg_status bsg_set_wm_update(bsg_ctx *ctx, int32_t chain, int32_t enable) {
                 "subject (an intercept or a full set of group indicators)");
   if (enable && !(d.dev.wm2 > 0.0))
     return fail(ctx, BSG_ERR_INVALID, "the beta_WM update needs a nonzero WM map");
+  if (enable && c.dev.model != 1)
+    return fail(ctx, BSG_ERR_UNSUPPORTED, "the beta_WM update is probit only");
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   const int32_t on = enable ? 1 : 0;
@@ -1167,22 +1210,36 @@ size_t ckpt_bytes_v1(const Dataset &d) {
          sizeof(double) * ((size_t)2 * d.P * d.V + (size_t)d.S * d.V);
 }
 
-size_t ckpt_bytes(const Dataset &d) {
+struct MixCkpt {  // link (MODEL); its weights phi follow unless probit
+  int32_t model, pad;
+};
+
+// Version 2 layout: the v1 body, PredCkpt, Qhat [N][max(S,1)], WmCkpt,
+// MixCkpt, then phi [N][n_0] and [N][n_1] for the t/logit links.
+size_t ckpt_fixed(const Dataset &d) {
   return ckpt_bytes_v1(d) + sizeof(PredCkpt) +
-         sizeof(double) * (size_t)d.N * std::max(d.S, 1) + sizeof(WmCkpt);
+         sizeof(double) * (size_t)d.N * std::max(d.S, 1) + sizeof(WmCkpt) +
+         sizeof(MixCkpt);
+}
+
+size_t ckpt_bytes(const Dataset &d, int model) {
+  return ckpt_fixed(d) + (model != 1 ? sizeof(float) * (size_t)d.N *
+                                           (d.vox[0].size() + d.vox[1].size())
+                                     : 0);
 }
 }  // namespace
 
 int64_t bsg_checkpoint_size(const bsg_ctx *ctx, int32_t chain) {
   if (!valid_chain(ctx, chain)) return -1;
-  return (int64_t)ckpt_bytes(ctx->ds[ctx->ch[chain].dataset]);
+  return (int64_t)ckpt_bytes(ctx->ds[ctx->ch[chain].dataset], ctx->ch[chain].dev.model);
 }
 
 bsg_status bsg_checkpoint(bsg_ctx *ctx, int32_t chain, void *buf, int64_t size) {
   if (!valid_chain(ctx, chain) || !buf) return BSG_ERR_INVALID;
   const Chain &c = ctx->ch[chain];
   const Dataset &d = ctx->ds[c.dataset];
-  if (size < (int64_t)ckpt_bytes(d)) return fail(ctx, BSG_ERR_INVALID, "buffer too small");
+  if (size < (int64_t)ckpt_bytes(d, c.dev.model))
+    return fail(ctx, BSG_ERR_INVALID, "buffer too small");
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   char *p = static_cast<char *>(buf);
@@ -1219,6 +1276,13 @@ bsg_status bsg_checkpoint(bsg_ctx *ctx, int32_t chain, void *buf, int64_t size) 
   }
   const WmCkpt wk{c.dev.wm_update, 0, ws.sum};
   std::memcpy(p, &wk, sizeof(wk));
+  p += sizeof(wk);
+  const MixCkpt mk{c.dev.model, 0};
+  std::memcpy(p, &mk, sizeof(mk));
+  p += sizeof(mk);
+  if (c.dev.model != 1)
+    for (int k = 0; k < 2; ++k)
+      CK(get(c.dev.phi[k], sizeof(float) * (size_t)d.N * d.vox[k].size()));
   return BSG_OK;
 }
 
@@ -1232,8 +1296,15 @@ bsg_status bsg_restore(bsg_ctx *ctx, int32_t chain, const void *buf, int64_t siz
   if (h.magic != kCkptMagic || (h.version != 1 && h.version != 2))
     return fail(ctx, BSG_ERR_INVALID, "not a checkpoint");
   if (h.P != d.P || h.Vp != d.Vp || h.V != d.V || h.S != d.S ||
-      size < (int64_t)(h.version == 1 ? ckpt_bytes_v1(d) : ckpt_bytes(d)))
+      size < (int64_t)(h.version == 1 ? ckpt_bytes_v1(d) : ckpt_fixed(d)))
     return fail(ctx, BSG_ERR_INVALID, "checkpoint is for a study of another shape");
+  MixCkpt mk{1, 0};
+  if (h.version == 2) {
+    std::memcpy(&mk, static_cast<const char *>(buf) + ckpt_fixed(d) - sizeof(MixCkpt),
+                sizeof(mk));
+    if (mk.model < 0 || mk.model > 2 || size < (int64_t)ckpt_bytes(d, mk.model))
+      return fail(ctx, BSG_ERR_INVALID, "checkpoint is for a study of another shape");
+  }
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   const char *p = static_cast<const char *>(buf) + sizeof(h);
@@ -1258,23 +1329,24 @@ bsg_status bsg_restore(bsg_ctx *ctx, int32_t chain, const void *buf, int64_t siz
     std::memcpy(&pk, p, sizeof(pk));
     p += sizeof(pk);
   }
+  const size_t nq = (size_t)d.N * std::max(d.S, 1);
   if (pk.allocated || c.dev.pred_part) {
     bsg_status ps = ensure_pred(ctx, c);
     if (ps) return ps;
-    const size_t nq = (size_t)d.N * std::max(d.S, 1);
     if (pk.allocated)
-      CK(put(c.dev.qhat, sizeof(double) * nq));
+      CK(cudaMemcpy(c.dev.qhat, p, sizeof(double) * nq, cudaMemcpyHostToDevice));
     else
       CK(cudaMemset(c.dev.qhat, 0, sizeof(double) * nq));
     CK(cudaMemcpy(c.dev.npred, &pk.npred, sizeof(long long), cudaMemcpyHostToDevice));
     const double sums[2] = {pk.ed_sum, 0.0};
     CK(cudaMemcpy(c.dev.pred_sums, sums, sizeof(sums), cudaMemcpyHostToDevice));
   }
+  if (h.version == 2) p += sizeof(double) * nq;
   c.pred_on = pk.on != 0;
   WmCkpt wk{0, 0, 0.0};
   if (h.version == 2) {
-    p = static_cast<const char *>(buf) + ckpt_bytes(d) - sizeof(WmCkpt);
     std::memcpy(&wk, p, sizeof(wk));
+    p += sizeof(wk) + sizeof(MixCkpt);
   } else {
     long long nk = 0;  // v1: beta_WM was fixed, so its kept sum is nk beta_WM
     CK(cudaMemcpy(&nk, c.dev.nkept, sizeof(nk), cudaMemcpyDeviceToHost));
@@ -1285,6 +1357,13 @@ bsg_status bsg_restore(bsg_ctx *ctx, int32_t chain, const void *buf, int64_t siz
   const WmState ws{wk.sum, h.beta_wm, 0};
   CK(cudaMemcpy(c.dev.wm_sum, &ws, sizeof(ws), cudaMemcpyHostToDevice));
   c.dev.wm_update = wk.update;
+  if (mk.model != c.dev.model) {
+    bsg_status ms = set_model(ctx, c, mk.model);
+    if (ms) return ms;
+  }
+  if (mk.model != 1)
+    for (int k = 0; k < 2; ++k)
+      CK(put(c.dev.phi[k], sizeof(float) * (size_t)d.N * d.vox[k].size()));
   c.desc.beta_wm = h.beta_wm;
   c.dev.df_offset = h.df_offset;
   c.dev.burnin = h.burnin;
@@ -1302,7 +1381,7 @@ bsg_status bsg_autotune(bsg_ctx *ctx, int32_t sweeps, int32_t *best_lpv,
   if (ctx->ch.empty()) return fail(ctx, BSG_ERR_STATE, "no chain");
   std::vector<std::vector<char>> saved(ctx->ch.size());
   for (size_t i = 0; i < ctx->ch.size(); ++i) {
-    saved[i].resize(ckpt_bytes(ctx->ds[ctx->ch[i].dataset]));
+    saved[i].resize(ckpt_bytes(ctx->ds[ctx->ch[i].dataset], ctx->ch[i].dev.model));
     bsg_status s = bsg_checkpoint(ctx, (int32_t)i, saved[i].data(), (int64_t)saved[i].size());
     if (s) return s;
   }
@@ -1346,6 +1425,8 @@ bsg_status bsg_sweep_supplied(bsg_ctx *ctx, int32_t chain, const uint32_t *ubits
   if (c.dev.wm_update)
     return fail(ctx, BSG_ERR_UNSUPPORTED,
                 "supplied-variate sweeps take beta_WM as given (turn its update off)");
+  if (c.dev.model != 1)
+    return fail(ctx, BSG_ERR_UNSUPPORTED, "supplied-variate sweeps are probit only");
   cudaError_t e;
   const int P = d.P, nw = P * (P - 1) / 2;
   Supplied sup{};
@@ -1380,6 +1461,17 @@ bsg_status bsg_sweep_supplied(bsg_ctx *ctx, int32_t chain, const uint32_t *ubits
                   (void *)dm1})
     dfree(ctx, p);
   return bsg_sync(ctx);
+}
+
+// ------------------------------------------------------------ the link --
+bsg_status bsg_set_model(bsg_ctx *ctx, int32_t chain, int32_t model) {
+  if (!valid_chain(ctx, chain) || model < 0 || model > 2) return BSG_ERR_INVALID;
+  Chain &c = ctx->ch[chain];
+  if (model != 1 && c.dev.wm_update)
+    return fail(ctx, BSG_ERR_UNSUPPORTED, "the beta_WM update is probit only");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return set_model(ctx, c, model);
 }
 
 // ------------------------------------------------ DIC / Qhat predictive --

@@ -135,6 +135,48 @@ static __device__ __noinline__ float tn_lower_tail(float a, uint32_t i, uint32_t
   return a;
 }
 
+// ------------------------------------------------ scale-mixture latent ----
+// One Marsaglia & Tsang (2000) attempt at Gamma(alpha, 1), alpha >= 1, with
+// d = alpha - 1/3 and c = 1/sqrt(9 d) from a normal (bits kn) and a uniform
+// (bits ku): g = d v^3 with v = 1 + c x, accepted by the squeeze
+// u < 1 - 0.0331 x^4 or by log u < x^2/2 + d (1 - v^3 + log v^3).
+__device__ __forceinline__ bool gamma_mt_try(float d, float c, uint32_t kn,
+                                             uint32_t ku, float *g) {
+  const float x = normal_of(kn);
+  const float v = fmaf(c, x, 1.f);
+  const float v3 = v * v * v;
+  *g = d * v3;
+  if (!(v > 0.f)) return false;
+  const float u = u_of(ku), x2 = x * x;
+  if (u < fmaf(-0.0331f * x2, x2, 1.f)) return true;
+  return lg2_approx(u) * 0.693147181f <
+         fmaf(0.5f, x2, d * (1.f - v3 + lg2_approx(v3) * 0.693147181f));
+}
+
+// Further attempts after a rejected first one: attempt pairs from counters
+// (i * 32 + q, v, sweep, c3), at most kGammaMax attempts in all; sets
+// *ok = 0 and returns d (the mode) if none is accepted.
+static __device__ __noinline__ float gamma_mt_more(float d, float c, uint32_t i,
+                                                   uint32_t v, uint32_t sweep,
+                                                   uint32_t c3, uint32_t key0,
+                                                   uint32_t key1, int *ok) {
+  float g = d;
+  for (int q = 0; q < (kGammaMax - 1) / 2; ++q) {
+    const uint4 r = philox1(make_uint4(i * 32u + (uint32_t)q, v, sweep, c3), key0, key1);
+    if (gamma_mt_try(d, c, r.x, r.y, &g)) return g;
+    if (gamma_mt_try(d, c, r.z, r.w, &g)) return g;
+  }
+  *ok = 0;
+  return d;
+}
+
+// Logistic lesion probability of the t/logit links (ProbLogitGPU,
+// covarGPU.cu:1695-1721): exp(x / lf) / (1 + exp(x / lf)), written so that
+// it cannot overflow.
+__device__ __forceinline__ float prob_logit(float x, float inv_lf) {
+  return 1.f / (1.f + expf(-x * inv_lf));
+}
+
 // Abramowitz & Stegun 26.2.17 normal CDF (covarGPU.cu:1672-1693 uses the
 // same published polynomial).
 __device__ __forceinline__ float prob_sdnorm(float x) {

@@ -26,17 +26,23 @@ namespace bsg {
 // Resident 256-thread blocks per SM asked of ptxas: three (85 registers) up
 // to P = 5, two (128 registers) above, measured fastest on the brain-sized
 // study; BSG_FUSED_MIN_BLOCKS overrides it for tuning builds.
-template <int P>
+template <int P, bool MIX = false>
 constexpr int fused_min_blocks() {
 #ifdef BSG_FUSED_MIN_BLOCKS
   return BSG_FUSED_MIN_BLOCKS;
 #else
-  return P <= 5 ? 3 : 2;
+  // the t/logit kernel also keeps the voxel's X' Phi X in registers
+  return MIX ? (P <= 5 ? 2 : 1) : (P <= 5 ? 3 : 2);
 #endif
 }
 
-template <int P, int LPV, bool SUPP>
-__global__ void __launch_bounds__(256, fused_min_blocks<P>())
+// MIX: the t/logit links (the reference's MODEL 0 and 2, Z_GPU2 and
+// Phi_GPU, covarGPU.cu:1430-1563, and the weighted Spat_Coef,
+// covarGPU.cu:398-513): Z_iv ~ N(mu, 1/phi_iv) truncated by Y, then
+// phi_iv | Z, beta ~ Gamma((nu + 1) / 2, rate (nu + (Z - mu)^2) / 2), and the
+// coefficient draw uses X' Phi X and X' Phi (Z - b_WM WM).
+template <int P, int LPV, bool SUPP, bool MIX = false>
+__global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
     fused_colour_kernel(const DatasetDev *__restrict__ dsv,
                         ChainDev *__restrict__ chv,
                         const BlockMap *__restrict__ map, int colour,
@@ -81,6 +87,10 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
   }
 #pragma unroll
   for (int p = 0; p < P; ++p) acc[p] = 0.f;
+  constexpr int NQ = MIX ? NT : 1;
+  float qw[NQ];  // MIX: this voxel's X' Phi X, packed lower
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) qw[q] = 0.f;
 
   PhiloxKey key;
   if (!SUPP) key.init(ch.key0, ch.key1);
@@ -99,7 +109,8 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
       // One subject: mu = bwm + x'beta; a = -mu if Y = 1 else mu (sign-bit
       // flip by ymask = Y << 31); t ~ N(0,1) on (a, inf);
       // Z - bwm = x'beta + (Y ? t : -t); acc += x (Z - bwm).
-      auto subject = [&](int col, uint32_t ymask, uint32_t kk, uint32_t isub) {
+      auto subject = [&](int col, uint32_t ymask, uint32_t kk, uint32_t isub,
+                         uint32_t gn, uint32_t gu) {
         float x[P];
         const float4 v0 = *reinterpret_cast<const float4 *>(&Xs[col][0]);
         x[0] = v0.x;
@@ -116,6 +127,39 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
         float m0 = 0.f;
 #pragma unroll
         for (int p = 0; p < P; ++p) m0 = fmaf(beta[p], x[p], m0);
+        if constexpr (MIX) {
+          // standardised: (Z - mu) sqrt(phi) ~ N(0, 1) on (a, inf) after the
+          // outcome's sign flip, a = -/+ mu sqrt(phi)
+          float *pp = ch.phi[colour] + (size_t)isub * nc + j;
+          const float ph = *pp;
+          const float sd = rsqrt_approx(ph);
+          const float a = __uint_as_float(__float_as_uint((m0 + bwm) * (ph * sd)) ^ ymask);
+          float t = tn_lower_inv(fminf(a, kATail), kk);
+          if (__any_sync(__activemask(), a > kATail) && a > kATail)
+            t = tn_lower_tail(a, isub, (uint32_t)v, sweep, cid | kTagZTail, ch.key0,
+                              ch.key1, &ok);
+          const float r = __uint_as_float(__float_as_uint(t * sd) ^ ymask ^ 0x80000000u);
+          const float zr = m0 + r;  // Z - b_WM WM
+          float gm;
+          if (!gamma_mt_try(ch.mix_d, ch.mix_c, gn, gu, &gm))
+            gm = gamma_mt_more(ch.mix_d, ch.mix_c, isub, (uint32_t)v, sweep,
+                               cid | kTagPhiMore, ch.key0, ch.key1, &ok);
+          const float phn = 2.f * gm / fmaf(r, r, ch.t_df);
+          *pp = phn;
+          const float wz = phn * zr;
+          float px[P];
+#pragma unroll
+          for (int p = 0; p < P; ++p) {
+            acc[p] = fmaf(x[p], wz, acc[p]);
+            px[p] = phn * x[p];
+          }
+#pragma unroll
+          for (int a2 = 0; a2 < P; ++a2)
+#pragma unroll
+            for (int b2 = 0; b2 <= a2; ++b2)
+              qw[tri(a2, b2)] = fmaf(px[a2], x[b2], qw[tri(a2, b2)]);
+          return;
+        }
         const float a = __uint_as_float(__float_as_uint(m0 + bwm) ^ ymask);
         float t;
         if (SUPP) {
@@ -143,15 +187,24 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
         const int nbits = min(32, cn - (wl << 5));
         const int xo = (wl << 5) + wl;  // padded offset of bit 0
         const uint32_t i00 = (uint32_t)(i0 + (wl << 5));
+        // MIX: the gamma variates of subjects i, i + 1 come from counter
+        // i / 2 (normal, uniform each)
+        auto gpair = [&](uint32_t i) -> uint4 {
+          if (!MIX) return make_uint4(0, 0, 0, 0);
+          return philox(make_uint4(i >> 1, (uint32_t)v, sweep, cid | kTagPhi), key);
+        };
         if (nbits == 32) {
 #pragma unroll 1
           for (int b = 0; b < 32; b += 4) {
             const uint32_t i = i00 + (uint32_t)b;
             uint4 r = make_uint4(0, 0, 0, 0);
             if (!SUPP) r = philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key);
+            const uint4 g0 = gpair(i), g1 = gpair(i + 2);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-              subject(xo + b + q, yw << 31, variate(r, q, i + q), i + q);
+              const uint4 gq = q < 2 ? g0 : g1;
+              subject(xo + b + q, yw << 31, variate(r, q, i + q), i + q,
+                      (q & 1) ? gq.z : gq.x, (q & 1) ? gq.w : gq.y);
               yw >>= 1;
             }
           }
@@ -160,9 +213,13 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
             const uint32_t i = i00 + (uint32_t)b;
             uint4 r = make_uint4(0, 0, 0, 0);
             if (!SUPP) r = philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key);
+            const uint4 g0 = gpair(i), g1 = gpair(i + 2);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-              if (b + q < nbits) subject(xo + b + q, yw << 31, variate(r, q, i + q), i + q);
+              const uint4 gq = q < 2 ? g0 : g1;
+              if (b + q < nbits)
+                subject(xo + b + q, yw << 31, variate(r, q, i + q), i + q,
+                        (q & 1) ? gq.z : gq.x, (q & 1) ? gq.w : gq.y);
               yw >>= 1;
             }
           }
@@ -225,7 +282,9 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
       for (int q = 0; q < P; ++q) s += Om[q + a * P] * sumV[q];
       b[a] = s;
 #pragma unroll
-      for (int q = 0; q <= a; ++q) Q[tri(a, q)] = Xtx[q + a * P] + nnb * Om[q + a * P];
+      for (int q = 0; q <= a; ++q)
+        Q[tri(a, q)] = (MIX ? qw[tri(a, q) < NQ ? tri(a, q) : 0] : Xtx[q + a * P]) +
+                       nnb * Om[q + a * P];
     }
     bool okc = chol_packed<P>(Q);
 
@@ -321,7 +380,8 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
 #pragma unroll
       for (int g2 = 0; g2 < P; ++g2)
         if (g2 < d.S)
-          ch.prb_sum[(size_t)g2 * d.V + v] += (double)prob_sdnorm(bnew[g2] + bwm);
+          ch.prb_sum[(size_t)g2 * d.V + v] +=
+              (double)(MIX ? prob_logit(bnew[g2], ch.inv_lf) : prob_sdnorm(bnew[g2] + bwm));
     }
 
     // ---- Omega pair products (Spat_Coef_Prec, covarGPU.cu:953-1013) -----
@@ -446,7 +506,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P>())
 // programmatic-stream-serialization attribute, so it may start once every
 // block of the previous kernel in the stream has passed its dependency
 // point.
-template <int P, int LPV, bool SUPP>
+template <int P, int LPV, bool SUPP, bool MIX = false>
 cudaError_t launch_one(int nblocks, int threads, cudaStream_t st, bool pdl,
                        const DatasetDev *ds, ChainDev *ch, const BlockMap *map,
                        int colour, const Supplied &sup) {
@@ -460,7 +520,7 @@ cudaError_t launch_one(int nblocks, int threads, cudaStream_t st, bool pdl,
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = pdl ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, fused_colour_kernel<P, LPV, SUPP>, ds, ch, map,
+  return cudaLaunchKernelEx(&cfg, fused_colour_kernel<P, LPV, SUPP, MIX>, ds, ch, map,
                             colour, sup);
 }
 

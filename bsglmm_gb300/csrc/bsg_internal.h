@@ -40,6 +40,8 @@ enum : uint32_t {
   kTagWNorm = 4,
   kTagGamma = 5,
   kTagWm = 6,
+  kTagPhi = 7,      // scale-mixture weight draws (t/logit links)
+  kTagPhiMore = 8,  // their further attempts
 };
 
 // Sticky per-chain error bits (ChainDev::status).
@@ -77,6 +79,13 @@ struct ChainDev {
   float *wm_beta;          // [1] beta_WM, the white-matter coefficient
   double *wm_sum;          // [1] sum of beta_WM over kept sweeps
   int32_t wm_update;       // draw beta_WM | Z, beta every sweep
+  // Link (the reference's MODEL, main.cu:42,168-175): 1 probit; 0 logistic
+  // and 2 t, both as a t scale mixture of normals with weights phi.
+  int32_t model;
+  float t_df;              // nu of the t link (8 logistic, 3 t)
+  float inv_lf;            // 1 / logit_factor (0.634 logistic, 1 t)
+  float mix_d, mix_c;      // Marsaglia-Tsang d, c of Gamma((nu + 1) / 2)
+  float *phi[2];           // [N][n_c] per colour: weights (t/logit links)
   int32_t df_offset, burnin, thin;
   float *beta;             // [P][Vp]
   float *omega_f;          // [P*P] float copy read by the colour kernels
@@ -126,8 +135,13 @@ cudaError_t launch_fused(int P, int lpv, int threads, bool supplied,
                          const BlockMap *map, int nblocks, int colour,
                          const Supplied &sup, cudaStream_t st,
                          bool pdl = false);
+// The colour kernel of the t/logit links (one lane per voxel, Philox).
+cudaError_t launch_fused_mix(int P, int threads, const DatasetDev *ds, ChainDev *ch,
+                             const BlockMap *map, int nblocks, int colour,
+                             cudaStream_t st, bool pdl);
 cudaError_t launch_prb(const DatasetDev *ds, const ChainDev *ch, int chain,
                        const DatasetDev &dh, float *prb, cudaStream_t st);
+cudaError_t launch_fill(float *p, size_t n, float value, cudaStream_t st);
 cudaError_t launch_pack(const uint8_t *bytes, int N, int V, int nc,
                         const int32_t *vidx, uint32_t *ybits, int *status,
                         cudaStream_t st);

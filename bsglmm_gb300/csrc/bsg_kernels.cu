@@ -1,5 +1,7 @@
 // bsg_kernels.cu -- dispatcher of the fused colour kernel, the
 // lesion-probability map and outcome bit packing.
+#include <algorithm>
+
 #include "bsg_device.cuh"
 
 namespace bsg {
@@ -60,8 +62,12 @@ __global__ void prb_kernel(const DatasetDev *__restrict__ dsv,
     const int j = c ? pos - n0 : pos;
     const int sc = d.nb[c][j], v = d.vidx[c][j];
     const float bwm = *ch.wm_beta * (d.wm ? d.wm[v] : 1.f);
-    for (int g = 0; g < d.S; ++g)
-      prb[(size_t)g * d.V + v] = prob_sdnorm(ch.beta[(size_t)g * d.Vp + sc] + bwm);
+    for (int g = 0; g < d.S; ++g) {
+      const float b = ch.beta[(size_t)g * d.Vp + sc];
+      // t/logit links: ProbLogitGPU (covarGPU.cu:1695-1721), without WM
+      prb[(size_t)g * d.V + v] = ch.model != 1 ? prob_logit(b, ch.inv_lf)
+                                               : prob_sdnorm(b + bwm);
+    }
   }
 }
 
@@ -71,6 +77,20 @@ cudaError_t launch_prb(const DatasetDev *ds, const ChainDev *ch, int chain,
   if (ntot <= 0) return cudaSuccess;
   const int blocks = (ntot + 255) / 256;
   prb_kernel<<<blocks, 256, 0, st>>>(ds, ch, chain, prb);
+  return cudaGetLastError();
+}
+
+// ----------------------------------------------------------------- fill --
+__global__ void fill_kernel(float *p, size_t n, float value) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    p[i] = value;
+}
+
+cudaError_t launch_fill(float *p, size_t n, float value, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const size_t blocks = std::min<size_t>((n + 255) / 256, 8192);
+  fill_kernel<<<(unsigned)blocks, 256, 0, st>>>(p, n, value);
   return cudaGetLastError();
 }
 

@@ -59,6 +59,14 @@ __device__ __forceinline__ float log2lik_as(float a) {
   return lg2_approx(u) + (tail ? w : 0.f);
 }
 
+// log2 P(Y | eta) for the t/logit links, P(Y = 1) = 1 / (1 + exp(-z)) with
+// z = eta / lf (ProbLogitGPU_prediction, covarGPU.cu:1750-1781), for a = z
+// with its sign flipped when Y = 0: -log2(1 + exp(-a)).
+__device__ __forceinline__ float log2lik_logit(float a) {
+  const float e = ex2_approx(fabsf(a) * -1.44269504f);
+  return -(lg2_approx(1.f + e) + fmaxf(-a, 0.f) * 1.44269504f);
+}
+
 __device__ __forceinline__ bool predict_gate(const ChainDev &ch, int mode) {
   if (mode != kPredKept) return true;
   const long long s = ch.sweep[1] - 1;  // the sweep that just completed
@@ -101,6 +109,10 @@ __global__ void __launch_bounds__(kPredThreads)
   const double inv_nk = de ? 1.0 / (double)(*ch.nkept > 0 ? *ch.nkept : 1) : 0.0;
   // beta_WM: the current value, or its mean over kept sweeps for DE (MWM)
   const float bwc = de ? (float)(*ch.wm_sum * inv_nk) : *ch.wm_beta;
+  // t/logit links: logistic of eta / lf; the DE of compute_prb_DIC
+  // (covar.cpp:457-465) takes exp(eta) / (1 + exp(eta)), without lf
+  const bool logit = ch.model != 1;
+  const float ilf = de ? 1.f : ch.inv_lf;
 
   const int t0 = tile * tw, t1 = min(t0 + tw, ntot);
   for (int q0 = t0; q0 < t1; q0 += kPredSub) {
@@ -153,14 +165,17 @@ __global__ void __launch_bounds__(kPredThreads)
             float eta = b[P];
 #pragma unroll
             for (int p = 0; p < P; ++p) eta = fmaf(b[p], x[p], eta);
-            s32[0] += log2lik_as(__uint_as_float(__float_as_uint(eta) ^ ymask));
+            const float a = __uint_as_float(__float_as_uint(eta) ^ ymask);
+            s32[0] += logit ? log2lik_logit(a) : log2lik_as(a);
           } else {
             float rest = b[P];
 #pragma unroll
             for (int p = S; p < P; ++p) rest = fmaf(b[p], x[p], rest);
 #pragma unroll
-            for (int g = 0; g < S; ++g)
-              s32[g] += log2lik_as(__uint_as_float(__float_as_uint(b[g] + rest) ^ ymask));
+            for (int g = 0; g < S; ++g) {
+              const float a = __uint_as_float(__float_as_uint(b[g] + rest) ^ ymask);
+              s32[g] += logit ? log2lik_logit(a * ilf) : log2lik_as(a);
+            }
           }
         }
 #pragma unroll

@@ -24,7 +24,9 @@
 //   compute_predictGPU    runs the library's predictive pass on the current
 //                         coefficients and updates the host Qhat;
 //   updateBetaGPU         turns on the library's beta_WM draw (at the end of
-//                         each sweep) and returns the latest beta_WM.
+//                         each sweep) and returns the latest beta_WM;
+//   updatePhiGPU          nothing: with MODEL != 1 the chain runs the t/logit
+//                         link, whose weights are drawn inside the sweep.
 // The Wishart degrees of freedom follow the reference GPU path,
 // df = TOTVOX + 19 (covarGPU.cu:1104).
 #include <cuda_runtime.h>
@@ -107,6 +109,8 @@ bool ensure(const float *covar, const float *WM, unsigned long *seed) {
   cd.thin = 1;
   cd.beta_wm = g.beta;
   report("bsg_add_chain", s = bsg_add_chain(g.ctx, g.ds, &cd, &g.ch));
+  if (s == BSG_OK && MODEL != 1)  // t/logit links (main.cu:42,168-175)
+    report("bsg_set_model", s = bsg_set_model(g.ctx, g.ch, MODEL));
   return s == BSG_OK;
 }
 
@@ -217,12 +221,13 @@ void updateBetaGPU(float *beta, float *, float *, float *, float *, float, float
   *beta = b;
 }
 
-// Paths the reference never takes with its shipped settings (probit
-// MODEL = 1, NCOV_FIX = 0): defined so the program links, they report that
-// they are unsupported.
-void updatePhiGPU(float, float *) {
-  std::fprintf(stderr, "bsglmm_gb300 shim: MODEL != 1 is not supported\n");
-}
+// updatePhiGPU (covarGPU.cu:1565-1588, MODEL != 1): the weights phi of the
+// t/logit links are drawn inside the sweep, right after each latent draw,
+// so there is nothing left to do here.
+void updatePhiGPU(float, float *) {}
+
+// A path the reference never takes with its shipped settings (NCOV_FIX =
+// 0): defined so the program links, it reports that it is unsupported.
 void updatefixMeanGPU(float *, float, float *, float *, float *, float,
                       unsigned long *) {
   std::fprintf(stderr, "bsglmm_gb300 shim: NCOV_FIX > 0 is not supported\n");

@@ -231,6 +231,15 @@ class Sampler:
         self._check(self._L.bsg_reset_accumulators(self._h, chain),
                     "bsg_reset_accumulators")
 
+    # --------------------------------------------------------- the link --
+    MODELS = {"logistic": 0, "probit": 1, "t": 2}
+
+    def set_model(self, chain: int = 0, model="probit"):
+        """Latent link of the chain: "probit" (default), "logistic" or "t"
+        (the reference's MODEL 1, 0, 2), or the MODEL number."""
+        m = self.MODELS[model] if isinstance(model, str) else int(model)
+        self._check(self._L.bsg_set_model(self._h, chain, m), "bsg_set_model")
+
     # ------------------------------------------------ beta_WM update --
     def set_wm_update(self, chain: int = 0, enable: bool = True):
         """Draw beta_WM | Z, beta every sweep (updateBetaGPU)."""

@@ -134,6 +134,17 @@ bsg_status bsg_set_beta_wm(bsg_ctx *ctx, int32_t chain, float beta_wm);
  * to 1 for every subject (BSG_ERR_UNSUPPORTED otherwise) and a nonzero WM.
  * Off by default; kept in checkpoints. */
 bsg_status bsg_set_wm_update(bsg_ctx *ctx, int32_t chain, int32_t enable);
+/* Link of the chain's latent model, the reference's compile-time MODEL
+ * (main.cu:42,168-175): 1 probit (default); 0 logistic and 2 t, both as a t
+ * scale mixture of normals (nu = 8 with logit_factor 0.634, nu = 3 with 1):
+ * Z_iv ~ N(eta, 1 / phi_iv) truncated by Y, phi_iv ~ Gamma((nu + 1) / 2,
+ * (nu + (Z - eta)^2) / 2), the coefficient draw weighted by phi (Z_GPU2,
+ * Phi_GPU, Spat_Coef, covarGPU.cu:398-513,1430-1563).  The weights (N V
+ * floats) start at 1 and are kept in checkpoints.  Lesion probabilities are
+ * 1 / (1 + exp(-beta_g / logit_factor)) (ProbLogitGPU, covarGPU.cu:1695-1721).
+ * The t/logit links take production (Philox) variates only and no beta_WM
+ * update. */
+bsg_status bsg_set_model(bsg_ctx *ctx, int32_t chain, int32_t model);
 /* Current beta_WM and its mean over kept sweeps (the bWM map of
  * mcmc.cpp:795-840 is that mean times WM_v).  Either pointer may be NULL. */
 bsg_status bsg_get_beta_wm(bsg_ctx *ctx, int32_t chain, float *beta_wm,

@@ -367,9 +367,11 @@ void orc_update_z(const orc_problem *pb, double beta_wm,
 /* One voxel of Spat_Coefff (covar.cpp:137-181) in FP64: b = X'(Z - bWM) +
  * Omega s, Q = X'X + n_v Omega, then the MVN draw.  Returns 0 on a failed
  * Cholesky (beta left unchanged). */
+/* qw: X' Phi X of the voxel (t/logit links, Spat_Coef covarGPU.cu:398-513)
+ * or NULL for X'X. */
 static int beta_voxel(const orc_problem *pb, int c, int j, const double *b_in,
                       const double *omega, const double *e, int form,
-                      double *spatcoef) {
+                      double *spatcoef, const double *qw) {
   int P = pb->P, Vp = pb->Vp;
   int vox = pb->vox[c][j], sc = pb->idxsc[vox];
   double b[16], sumV[16], Q[256], W[256], m[16], out[16];
@@ -384,7 +386,8 @@ static int beta_voxel(const orc_problem *pb, int c, int j, const double *b_in,
   for (int a = 0; a < P; ++a)
     for (int q = 0; q < P; ++q) {
       b[a] += omega[q + a * P] * sumV[q];
-      Q[q + a * P] = (double)pb->xtx[q + a * P] + nb * omega[q + a * P];
+      Q[q + a * P] = (qw ? qw[q + a * P] : (double)pb->xtx[q + a * P]) +
+                     nb * omega[q + a * P];
     }
   if (!chol_lower(Q, P)) return 0;
   if (form == 0) {
@@ -436,7 +439,7 @@ int orc_update_spatcoef(const orc_problem *pb, double beta_wm,
         b[p] = s;
         e[p] = normals[(size_t)v * P + p];
       }
-      if (!beta_voxel(pb, c, j, b, omega, e, form, (double *)spatcoef))
+      if (!beta_voxel(pb, c, j, b, omega, e, form, (double *)spatcoef, NULL))
         fails++;
     }
   return fails;
@@ -550,8 +553,14 @@ double orc_loglik_as(double eta, int y) {
  * i.e. subject i's prediction as a member of group column g.  The
  * reference's y log(p + 1e-35) + (1 - y) log(1 - p + 1e-35) in FP32 is the
  * same quantity up to its guard and its cancellation when 1 - p < 2^-24. */
+/* log P(Y = y | z) with P(Y = 1) = 1 / (1 + exp(-z)). */
+static double loglik_logit(double z, int y) {
+  double a = y ? z : -z;  /* log sigma(a) = -log(1 + exp(-a)) */
+  return a >= 0 ? -log1p(exp(-a)) : a - log1p(exp(a));
+}
+
 void orc_predict(const orc_problem *pb, double beta_wm, const double *spatcoef,
-                 double *mpredict) {
+                 double *mpredict, int model, double inv_lf) {
   int N = pb->N, P = pb->P, S = pb->S, V = pb->V, Vp = pb->Vp;
   for (int i = 0; i < N * S; ++i) mpredict[i] = 0.0;
   for (int q = 0; q < pb->nsize; ++q) {
@@ -563,9 +572,12 @@ void orc_predict(const orc_problem *pb, double beta_wm, const double *spatcoef,
       for (int p = S; p < P; ++p)
         rest += spatcoef[(size_t)p * Vp + sc] * (double)pb->covar[(size_t)p * N + i];
       int y = pb->data[(size_t)i * V + v] != 0;
-      for (int g = 0; g < S; ++g)
+      for (int g = 0; g < S; ++g) {
+        double eta = spatcoef[(size_t)g * Vp + sc] + rest;
+        /* t/logit links: ProbLogitGPU_prediction, covarGPU.cu:1750-1781 */
         mpredict[(size_t)i * S + g] +=
-            orc_loglik_as(spatcoef[(size_t)g * Vp + sc] + rest, y);
+            model != 1 ? loglik_logit(eta * inv_lf, y) : orc_loglik_as(eta, y);
+      }
     }
   }
 }
@@ -577,7 +589,8 @@ void orc_predict(const orc_problem *pb, double beta_wm, const double *spatcoef,
  * covariates) and mwm[v] = mean of beta_WM WM_v.  The reference rounds eta
  * to float before its FP64 A&S evaluation, and its 1 - x cancels for
  * eta > 5 (relative error 1e-16 / (1 - x)); both are kept here. */
-double orc_dic_de(const orc_problem *pb, const double *mean, const double *mwm) {
+double orc_dic_de(const orc_problem *pb, const double *mean, const double *mwm,
+                  int model) {
   int N = pb->N, P = pb->P, V = pb->V;
   double de = 0.0;
   for (int i = 0; i < N; ++i)
@@ -585,7 +598,13 @@ double orc_dic_de(const orc_problem *pb, const double *mean, const double *mwm) 
       double y = 0.0;
       for (int p = 0; p < P; ++p)
         y += mean[(size_t)p * V + v] * (double)pb->covar[(size_t)p * N + i];
-      double x = orc_prob_sdnorm((double)(float)(y + (mwm ? mwm[v] : 0.0)));
+      double x;
+      if (model != 1) { /* covar.cpp:457-465: exp(eta) / (1 + exp(eta)) */
+        x = exp(y + (mwm ? mwm[v] : 0.0));
+        x /= (1.0 + x);
+      } else {
+        x = orc_prob_sdnorm((double)(float)(y + (mwm ? mwm[v] : 0.0)));
+      }
       int t = pb->data[(size_t)i * V + v];
       de += t * log(x + DBL_MIN) + (1 - t) * log(1.0 - x + DBL_MIN);
     }
@@ -654,11 +673,60 @@ static int chain_wishart(const orc_problem *pb, const orc_chain_cfg *cfg,
   return err;
 }
 
+/* One Marsaglia & Tsang (2000) attempt at Gamma(alpha, 1), alpha >= 1, with
+ * d = alpha - 1/3, c = 1/sqrt(9 d), from a normal and a uniform (bits kn,
+ * ku); the squeeze u < 1 - 0.0331 x^4 first, then log u < x^2/2 + d (1 -
+ * v^3 + log v^3).  The same test as the GPU's scale-mixture draw. */
+static int mt_try(double d, double c, uint32_t kn, uint32_t ku, double *g) {
+  double x = orc_normal_from_bits(kn), v = 1.0 + c * x, v3 = v * v * v;
+  *g = d * v3;
+  if (!(v > 0.0)) return 0;
+  double u = orc_u_from_bits(ku), x2 = x * x;
+  if (u < 1.0 - 0.0331 * x2 * x2) return 1;
+  return log(u) < 0.5 * x2 + d * (1.0 - v3 + log(v3));
+}
+
+/* phi | Z, beta ~ Gamma((nu + 1) / 2, rate (nu + r^2) / 2) for subject i of
+ * voxel v: attempt 0 from counter (i / 2, v, sweep, PHI) (normal, uniform
+ * in the first or second pair of words), further attempt pairs from
+ * (i * 32 + q, v, sweep, PHI_MORE). */
+static double mix_gamma(const orc_chain_cfg *cfg, double d, double c, uint32_t i,
+                        uint32_t v, uint32_t sw, int *err) {
+  uint32_t o[4];
+  double g;
+  philox(i >> 1, v, sw, (cfg->chain << 8) | ORC_TAG_PHI, cfg->key0, cfg->key1, o);
+  if (mt_try(d, c, o[(i & 1) * 2], o[(i & 1) * 2 + 1], &g)) return g;
+  for (int q = 0; q < (ORC_GAMMA_MAX - 1) / 2; ++q) {
+    philox(i * 32u + (uint32_t)q, v, sw, (cfg->chain << 8) | ORC_TAG_PHI_MORE,
+           cfg->key0, cfg->key1, o);
+    if (mt_try(d, c, o[0], o[1], &g)) return g;
+    if (mt_try(d, c, o[2], o[3], &g)) return g;
+  }
+  *err |= ORC_ERR_GAMMA_CAP;
+  return d;
+}
+
+double orc_mix_gamma(double alpha, uint32_t i, uint32_t v, uint32_t sweep,
+                     uint32_t key0, uint32_t key1, uint32_t chain) {
+  orc_chain_cfg cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.key0 = key0;
+  cfg.key1 = key1;
+  cfg.chain = chain;
+  double d = alpha - 1.0 / 3.0;
+  int err = 0;
+  return mix_gamma(&cfg, d, 1.0 / sqrt(9.0 * d), i, v, sweep, &err);
+}
+
 int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
                   int64_t nsweeps, double *spatcoef, double *omega,
                   double *acc_sum, double *acc_sq, double *prb_sum,
-                  int64_t *nkept, double *beta_wm, double *wm_sum) {
+                  int64_t *nkept, double *beta_wm, double *wm_sum,
+                  double *phi) {
   int N = pb->N, P = pb->P, V = pb->V, Vp = pb->Vp, S = pb->S, err = 0;
+  const int mix = cfg->model != 1 && phi;
+  const double nu = cfg->t_df, md = 0.5 * (nu + 1.0) - 1.0 / 3.0;
+  const double mc = 1.0 / sqrt(9.0 * md);
   uint32_t k0 = cfg->key0, k1 = cfg->key1, ch = cfg->chain;
   double *prb = (double *)malloc(sizeof(double) * ((size_t)S * V + 1));
   double bw = beta_wm ? *beta_wm : cfg->beta_wm;
@@ -673,7 +741,7 @@ int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
       for (int j = 0; j < pb->n[c]; ++j) {
         int vox = pb->vox[c][j], v = pb->idx[vox], sc = pb->idxsc[vox];
         double bwm = bw * pb->wm[v];
-        double b[16] = {0}, e[16], zs = 0.0;
+        double b[16] = {0}, e[16], zs = 0.0, qw[256] = {0};
         uint32_t o[4];
         for (int i = 0; i < N; ++i) {
           if ((i & 3) == 0)
@@ -683,7 +751,9 @@ int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
           for (int p = 0; p < P; ++p)
             mu += spatcoef[(size_t)p * Vp + sc] * pb->covar[p * N + i];
           int y = pb->data[(size_t)i * V + v] == 1;
-          double a = y ? -mu : mu, t;
+          /* t/logit links: (Z - mu) sqrt(phi) ~ N(0, 1) truncated */
+          double ph = mix ? phi[(size_t)i * V + v] : 1.0, sq = sqrt(ph);
+          double a = (y ? -mu : mu) * sq, t;
           if (a <= ORC_A_TAIL) {
             t = orc_tn_lower_inv(a, o[i & 3]);
           } else {
@@ -694,9 +764,20 @@ int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
             if (!orc_tn_lower_tail(a, kp, ORC_TAIL_MAX, &t))
               err |= ORC_ERR_TN_CAP;
           }
-          double z = y ? mu + t : mu - t;
+          double r = (y ? t : -t) / sq, z = mu + r;
           zs += z;
-          for (int p = 0; p < P; ++p) b[p] += pb->covar[p * N + i] * (z - bwm);
+          if (mix) {
+            double g = mix_gamma(cfg, md, mc, (uint32_t)i, (uint32_t)v, sw, &err);
+            double phn = 2.0 * g / (nu + r * r);
+            phi[(size_t)i * V + v] = phn;
+            for (int p = 0; p < P; ++p) {
+              double xp = pb->covar[p * N + i];
+              b[p] += xp * phn * (z - bwm);
+              for (int q = 0; q < P; ++q) qw[q + p * P] += phn * xp * pb->covar[q * N + i];
+            }
+          } else {
+            for (int p = 0; p < P; ++p) b[p] += pb->covar[p * N + i] * (z - bwm);
+          }
         }
         for (int p = 0; p < P; p += 4) {
           philox((uint32_t)(p >> 2), (uint32_t)v, sw, (ch << 8) | ORC_TAG_BETA,
@@ -704,7 +785,7 @@ int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
           for (int r = 0; r < 4 && p + r < P; ++r)
             e[p + r] = orc_normal_from_bits(o[r]);
         }
-        if (!beta_voxel(pb, c, j, b, omega, e, 1, spatcoef))
+        if (!beta_voxel(pb, c, j, b, omega, e, 1, spatcoef, mix ? qw : NULL))
           err |= ORC_ERR_CHOL;
         double xb = 0.0;
         for (int p = 0; p < P; ++p) xb += xsum[p] * spatcoef[(size_t)p * Vp + sc];
@@ -724,7 +805,15 @@ int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
     int kept = (s > cfg->burnin) && (s % (cfg->thin > 0 ? cfg->thin : 1) == 0);
     if (kept && wm_sum) *wm_sum += bw;
     if (kept && acc_sum) { /* running sums of mcmc.cpp:637-645 */
-      orc_compute_prb(pb, bw_used, spatcoef, prb);
+      if (mix) /* ProbLogitGPU (covarGPU.cu:1695-1721) */
+        for (int q = 0; q < pb->nsize; ++q) {
+          if (!pb->msk[q]) continue;
+          for (int g = 0; g < S; ++g)
+            prb[(size_t)g * V + pb->idx[q]] =
+                1.0 / (1.0 + exp(-spatcoef[(size_t)g * Vp + pb->idxsc[q]] * cfg->inv_lf));
+        }
+      else
+        orc_compute_prb(pb, bw_used, spatcoef, prb);
       ++(*nkept);
       for (int p = 0; p < pb->nsize; ++p) {
         if (!pb->msk[p]) continue;

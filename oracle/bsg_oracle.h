@@ -94,10 +94,12 @@ double orc_loglik_as(double eta, int y);
 /* compute_predictGPU (covarGPU.cu:1783-1903): mpredict[i*S + g], the log
  * predictive of subject i's outcomes as a member of group column g. */
 void orc_predict(const orc_problem *pb, double beta_wm, const double *spatcoef,
-                 double *mpredict);
+                 double *mpredict, int model, double inv_lf);
 /* compute_prb_DIC (covar.cpp:442-486): DE at the posterior means
- * mean[p*V + v] with mwm[v] (NULL = 0). */
-double orc_dic_de(const orc_problem *pb, const double *mean, const double *mwm);
+ * mean[p*V + v] with mwm[v] (NULL = 0); model != 1 takes its logistic
+ * branch. */
+double orc_dic_de(const orc_problem *pb, const double *mean, const double *mwm,
+                  int model);
 /* Column means (covarGPU.cu:563-583): sum over Vp entries / V. */
 void orc_col_means(const orc_problem *pb, const double *spatcoef,
                    double *means);
@@ -110,6 +112,8 @@ typedef struct {
   int32_t burnin, thin;   /* kept iff sweep > burnin && sweep % thin == 0 */
   double beta_wm;         /* initial beta_WM */
   int32_t wm_update;      /* draw beta_WM | Z, beta after both colours */
+  int32_t model;          /* 1 probit; 0 logistic, 2 t (scale mixture) */
+  double t_df, inv_lf;    /* nu and 1 / logit_factor of the t/logit links */
 } orc_chain_cfg;
 
 /* Runs sweeps [s0, s0 + nsweeps) from state (spatcoef, omega, *beta_wm) in
@@ -118,11 +122,18 @@ typedef struct {
  * beta_wm may be NULL (cfg->beta_wm, fixed).  Accumulates (if acc_sum !=
  * NULL) the running sums acc_sum[P][V], acc_sq[P][V], prb_sum[S][V] of
  * mcmc.cpp:637-645, *wm_sum (if not NULL, the kept beta_WM values) and
- * *nkept.  Returns an OR of error flags (0 = ok). */
+ * *nkept.  With model != 1, phi [N][V] holds the scale-mixture weights (in
+ * and out).  Returns an OR of error flags (0 = ok). */
 int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
                   int64_t nsweeps, double *spatcoef, double *omega,
                   double *acc_sum, double *acc_sq, double *prb_sum,
-                  int64_t *nkept, double *beta_wm, double *wm_sum);
+                  int64_t *nkept, double *beta_wm, double *wm_sum,
+                  double *phi);
+
+/* The scale-mixture Gamma(alpha, 1) draw of subject i at voxel v (the
+ * counters and Marsaglia-Tsang test the GPU uses). */
+double orc_mix_gamma(double alpha, uint32_t i, uint32_t v, uint32_t sweep,
+                     uint32_t key0, uint32_t key1, uint32_t chain);
 
 /* ------------------------------- CPU timing port of the reference sweep -- */
 /* A reentrant restatement of the reference's CPU sweep (mcmc.cpp:395-434:
@@ -150,6 +161,8 @@ int64_t orc_port_updates(const orc_port *pt, int nvox_limit);
 #define ORC_TAG_WNORM 4u
 #define ORC_TAG_GAMMA 5u
 #define ORC_TAG_WM 6u
+#define ORC_TAG_PHI 7u
+#define ORC_TAG_PHI_MORE 8u
 
 #define ORC_A_TAIL 5.0      /* inversion below, Robert rejection above */
 #define ORC_TAIL_MAX 16     /* rejection attempts per draw */

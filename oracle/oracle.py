@@ -72,9 +72,10 @@ def lib() -> C.CDLL:
             "orc_compute_prb": (None, [_P, _d, _P, _P]),
             "orc_col_means": (None, [_P, _P, _P]),
             "orc_loglik_as": (_d, [_d, _i]),
-            "orc_predict": (None, [_P, _d, _P, _P]),
-            "orc_dic_de": (_d, [_P, _P, _P]),
-            "orc_chain_run": (_i, [_P, _P, _i64, _i64, _P, _P, _P, _P, _P, _P, _P, _P]),
+            "orc_predict": (None, [_P, _d, _P, _P, _i, _d]),
+            "orc_dic_de": (_d, [_P, _P, _P, _i]),
+            "orc_mix_gamma": (_d, [_d, _u32, _u32, _u32, _u32, _u32, _u32]),
+            "orc_chain_run": (_i, [_P, _P, _i64, _i64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
             "orc_port_new": (_P, [_P, C.c_uint64, _i]),
             "orc_port_free": (None, [_P]),
             "orc_port_sweep": (None, [_P, _i]),
@@ -91,7 +92,8 @@ def lib() -> C.CDLL:
 class ChainCfg(C.Structure):
     _fields_ = [("key0", C.c_uint32), ("key1", C.c_uint32), ("chain", C.c_uint32),
                 ("df_offset", C.c_int32), ("burnin", C.c_int32), ("thin", C.c_int32),
-                ("beta_wm", C.c_double), ("wm_update", C.c_int32)]
+                ("beta_wm", C.c_double), ("wm_update", C.c_int32),
+                ("model", C.c_int32), ("t_df", C.c_double), ("inv_lf", C.c_double)]
 
 
 def philox(ctr, key) -> np.ndarray:
@@ -190,19 +192,20 @@ class Problem:
         self._L.orc_col_means(self.h, _p(b), _p(out))
         return out
 
-    def predict(self, spatcoef, beta_wm=0.0) -> np.ndarray:
+    def predict(self, spatcoef, beta_wm=0.0, model: int = 1) -> np.ndarray:
         """Mpredict [N][S] of compute_predictGPU (covarGPU.cu:1866-1903)."""
         b = np.ascontiguousarray(spatcoef, dtype=np.float64)
         out = np.zeros((self.N, self.S))
-        self._L.orc_predict(self.h, beta_wm, _p(b), _p(out))
+        inv_lf = 1.0 / 0.634 if model == 0 else 1.0
+        self._L.orc_predict(self.h, beta_wm, _p(b), _p(out), model, inv_lf)
         return out
 
-    def dic_de(self, mean, mwm=None) -> float:
+    def dic_de(self, mean, mwm=None, model: int = 1) -> float:
         """DE of compute_prb_DIC (covar.cpp:442-486) at the posterior means
         mean [P][V] and mwm [V] (None = 0)."""
         m = np.ascontiguousarray(mean, dtype=np.float64)
         w = None if mwm is None else np.ascontiguousarray(mwm, dtype=np.float64)
-        return self._L.orc_dic_de(self.h, _p(m), _p(w))
+        return self._L.orc_dic_de(self.h, _p(m), _p(w), model)
 
     def sweep_supplied(self, spatcoef, omega, ubits, normals, chi2, wnorm,
                        form=0, beta_wm=0.0):
@@ -216,12 +219,19 @@ class Problem:
 
     def chain(self, seed: int, nsweeps: int, chain_id: int = 0, burnin: int = 0,
               thin: int = 1, df_offset=None, beta_wm=0.0, s0: int = 0,
-              spatcoef=None, omega=None, wm_update: bool = False):
+              spatcoef=None, omega=None, wm_update: bool = False, model: int = 1,
+              phi=None):
         """FP64 chain on the sampler's counters.  Returns the state (beta,
-        omega, beta_wm) and the posterior summaries of the kept sweeps."""
+        omega, beta_wm, phi) and the posterior summaries of the kept sweeps.
+        model: the reference's MODEL (1 probit, 0 logistic, 2 t)."""
+        t_df, inv_lf = {0: (8.0, 1.0 / 0.634), 1: (1000.0, 1.0), 2: (3.0, 1.0)}[model]
         cfg = ChainCfg(seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF, chain_id,
                        self.P if df_offset is None else df_offset, burnin, thin,
-                       beta_wm, int(bool(wm_update)))
+                       beta_wm, int(bool(wm_update)), model, t_df, inv_lf)
+        ph = None
+        if model != 1:
+            ph = (np.ones((self.N, self.V)) if phi is None
+                  else np.array(phi, dtype=np.float64, order="C"))
         bw = C.c_double(beta_wm)
         wsum = C.c_double(0.0)
         b = (np.zeros((self.P, self.Vp)) if spatcoef is None
@@ -233,7 +243,7 @@ class Problem:
         nk = C.c_int64(0)
         err = self._L.orc_chain_run(self.h, C.byref(cfg), s0, nsweeps, _p(b), _p(om),
                                     _p(s1), _p(s2), _p(sp), C.byref(nk), C.byref(bw),
-                                    C.byref(wsum))
+                                    C.byref(wsum), _p(ph))
         T = nk.value
         with np.errstate(invalid="ignore", divide="ignore"):
             mean = s1 / T
@@ -242,7 +252,7 @@ class Problem:
             wm_mean = wsum.value / T if T else float("nan")
         return dict(beta=b, omega=om, mean=mean, var=var, prb=prb,
                     sum=s1, sumsq=s2, nkept=T, err=err, beta_wm=bw.value,
-                    wm_sum=wsum.value, wm_mean=wm_mean)
+                    wm_sum=wsum.value, wm_mean=wm_mean, phi=ph)
 
 
 def subtypes(covar, S: int) -> np.ndarray:
@@ -321,6 +331,7 @@ class _Ref:
         L.ref_prob_sdnorm.argtypes = [_d]
         L.ref_prob_sdnorm.restype = _d
         L.ref_compute_prb_dic.argtypes = [_P, _P, _P, _P]
+        L.ref_set_model.argtypes = [_i]
         L.ref_compute_prb_dic.restype = _d
         L.ref_cholesky_decomp.restype = _i
 
@@ -359,8 +370,9 @@ class _Ref:
     def prob_sdnorm(self, x: float) -> float:
         return self._L.ref_prob_sdnorm(x)
 
-    def compute_prb_dic(self, mean, mwm=None) -> float:
+    def compute_prb_dic(self, mean, mwm=None, model: int = 1) -> float:
         """The reference's compute_prb_DIC on posterior means [P][V]."""
+        self._L.ref_set_model(model)
         pb = self.pb
         R = pb.X * pb.Y * pb.Z
         lat = self._keep

@@ -195,6 +195,9 @@ void ref_compute_prb(float *prb, const float *spatcoef, const float *wm,
 
 double ref_prob_sdnorm(double x) { return ProbSDNorm(x); }
 
+/* The reference's MODEL global (main.cu:42). */
+void ref_set_model(int model) { MODEL = model; }
+
 /* covar.cpp:442-486: DE from the posterior-mean maps mcov[p][X*Y*Z] and
  * mwm[X*Y*Z] on the unpadded grid (x fastest), outcomes data[i*V + v]. */
 double ref_compute_prb_dic(double *mcov, double *mwm, float *covar,

@@ -5,14 +5,17 @@
 // sweep after the first, then writes the resulting Omega, coefficients,
 // lesion probabilities, the ED sum and Qhat.
 //
-// usage: shim_harness <study.bin> <sweeps> <out.bin> [wm]
+// usage: shim_harness <study.bin> <sweeps> <out.bin> [wm | model=M]
 // With "wm" the study file also holds V floats of WM after the seed and the
-// harness calls updateBetaGPU before each coefficient update (UPDATE_WM).
+// harness calls updateBetaGPU before each coefficient update (UPDATE_WM);
+// with "model=M" MODEL is M and updatePhiGPU follows updateZGPU
+// (mcmc.cpp:327-329).
 #include <cuda_runtime.h>
 
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 // ---- the reference's globals --------------------------------------------
@@ -39,6 +42,7 @@ void updateZGPU(unsigned char *, float, unsigned long *);
 void updateSpatCoefGPU(float *, float *, float *, float *, float *, float *,
                        float *, unsigned char *, float, float *, unsigned long *);
 void updateSpatCoefPrecGPU(float *, unsigned long *);
+void updatePhiGPU(float, float *);
 void updateBetaGPU(float *, float *, float *, float *, float *, float, float,
                    float *, float *, unsigned long *);
 void compute_prbGPU(float);
@@ -57,7 +61,9 @@ std::vector<T> rd(FILE *f, size_t n) {
 
 int main(int argc, char **argv) {
   if (argc != 4 && argc != 5) return 2;
-  UPDATE_WM = argc == 5;
+  UPDATE_WM = argc == 5 && std::string(argv[4]) == "wm";
+  if (argc == 5 && std::string(argv[4]).rfind("model=", 0) == 0)
+    MODEL = std::atoi(argv[4] + 6);
   FILE *f = std::fopen(argv[1], "rb");
   if (!f) return 2;
   auto hdr = rd<int32_t>(f, 8);
@@ -90,6 +96,7 @@ int main(int argc, char **argv) {
   int totsav = 0;
   for (int iter = 0; iter < sweeps; ++iter) {
     updateZGPU(data.data(), beta, seed);
+    if (MODEL != 1) updatePhiGPU(beta, nullptr);  // mcmc.cpp:327-329
     if (UPDATE_WM)  // mcmc.cpp:344-345
       updateBetaGPU(&beta, nullptr, nullptr, nullptr, nullptr, 0.f, 1e-6f, nullptr,
                     nullptr, seed);

@@ -151,3 +151,48 @@ def test_shim_wm_update_reproduces_native_chain(tmp_path):
         assert np.array_equal(om, prec)
         b_native, _ = s.beta_wm(ch)
     assert bwm_shim == b_native and bwm_shim != 0.0
+
+
+def test_shim_t_link_reproduces_native_chain(tmp_path):
+    """With MODEL = 2 (t link) the shimmed program runs the library's
+    scale-mixture chain: equal to the native chain with set_model(2)."""
+    import bsglmm_gb300 as bsg
+    from bsglmm_gb300 import synth
+    st = synth.small_study(75, shape=(9, 9, 8), N=40, P=3, S=1)
+    seed0 = [1111, 2222, 3333]
+    with bsg.Sampler() as s:
+        ds = s.add_dataset(st.mask, st.covar, st.data, 1)
+        info = s.info(ds)
+        lat = s.lattice(ds)
+    hdr = np.array([info["X"], info["Y"], info["Z"], info["N"], info["P"], info["S"],
+                    info["V"], info["Vp"]], np.int32)
+    study = tmp_path / "study.bin"
+    with open(study, "wb") as f:
+        for a in (hdr, lat["idx"].astype(np.int32), st.covar.astype(np.float32),
+                  st.data.astype(np.uint8), np.array(seed0, np.uint64)):
+            f.write(np.ascontiguousarray(a).tobytes())
+    exe = _build(tmp_path)
+    K = 4
+    out = tmp_path / "out.bin"
+    r = subprocess.run([str(exe), str(study), str(K), str(out), "model=2"],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    P, Vp = info["P"], info["Vp"]
+    raw = out.read_bytes()
+    prec = np.frombuffer(raw, np.float32, P * P, 0).reshape(P, P)
+    beta = np.frombuffer(raw, np.float32, P * Vp, 4 * P * P).reshape(P, Vp)
+    ks = list(seed0)
+    hi = int(_kiss(ks) * 4294967296.0)
+    lo = int(_kiss(ks) * 4294967296.0)
+    key = ((hi << 32) ^ lo) & ((1 << 64) - 1)
+    with bsg.Sampler() as s:
+        ds = s.add_dataset(st.mask, st.covar, st.data, 1)
+        ch = s.add_chain(ds, seed=key, df_offset=19, burnin=2**31 - 1)
+        s.set_model(ch, 2)
+        om = np.eye(P, dtype=np.float32)
+        for _ in range(K):
+            s.set_omega(ch, om.astype(np.float64))
+            s.run(1)
+            om = s.omega(ch).astype(np.float32)
+        assert np.array_equal(s.beta(ch), beta)
+        assert np.array_equal(om, prec)

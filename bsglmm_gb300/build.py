@@ -28,6 +28,7 @@ SOURCES = [
     "bsg_fused_l4.cu",
     "bsg_fused_l8.cu",
     "bsg_fused_mix.cu",
+    "bsg_fused_wm.cu",
     "bsg_kernels.cu",
     "bsg_peak.cu",
     "bsg_noalloc.cu",

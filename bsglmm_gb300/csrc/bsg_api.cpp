@@ -44,7 +44,7 @@ struct Chain {
 struct Group {
   int P = 0;
   bool mix = false;     // t/logit chains (scale-mixture colour kernel)
-  bool wm_any = false;  // a chain draws beta_WM: colour 0 waits for it
+  bool wm_any = false;  // its chains draw beta_WM: colour 0 waits for it
   std::vector<BlockMap> map[2];
   BlockMap *d_map[2] = {nullptr, nullptr};
   // predictive pass of the group's chains that have it on, one launch pair
@@ -300,19 +300,20 @@ bsg_status build_plan(bsg_ctx *ctx) {
   for (size_t ci = 0; ci < ctx->ch.size(); ++ci) {
     const Dataset &d = ctx->ds[ctx->ch[ci].dataset];
     const bool mix = ctx->ch[ci].dev.model != 1;
+    const bool wmu = ctx->ch[ci].dev.wm_update != 0;
     Group *g = nullptr;
     for (auto &gg : ctx->groups)
-      if (gg.P == d.P && gg.mix == mix) g = &gg;
+      if (gg.P == d.P && gg.mix == mix && gg.wm_any == wmu) g = &gg;
     if (!g) {
       ctx->groups.push_back(Group());
       g = &ctx->groups.back();
       g->P = d.P;
       g->mix = mix;
+      g->wm_any = wmu;
     }
-    // the t/logit kernel runs one lane per voxel
-    const int gvpb = mix ? ctx->threads : vpb;
+    // the t/logit and beta_WM kernels run one lane per voxel
+    const int gvpb = (mix || wmu) ? ctx->threads : vpb;
     for (int c = 0; c < 2; ++c) map_chain(g->map[c], (int)ci, (int)d.vox[c].size(), gvpb, c);
-    if (ctx->ch[ci].dev.wm_update) g->wm_any = true;
     if (ctx->ch[ci].pred_on) {
       const ChainDev &cv = ctx->ch[ci].dev;
       Group::Pred *pr = nullptr;
@@ -360,6 +361,9 @@ cudaError_t launch_colour(bsg_ctx *ctx, const Group &g, int c, cudaStream_t st, 
   if (g.mix)
     return launch_fused_mix(g.P, ctx->threads, ctx->d_ds, ctx->d_ch, g.d_map[c],
                             (int)g.map[c].size(), c, st, pdl);
+  if (g.wm_any)
+    return launch_fused_wm(g.P, ctx->threads, ctx->d_ds, ctx->d_ch, g.d_map[c],
+                           (int)g.map[c].size(), c, st, pdl);
   const Supplied sup{};
   return launch_fused(g.P, ctx->lpv, ctx->threads, false, ctx->d_ds, ctx->d_ch,
                       g.d_map[c], (int)g.map[c].size(), c, sup, st, pdl);
@@ -931,7 +935,8 @@ int64_t bsg_launches_per_sweep(const bsg_ctx *ctx) {
   std::vector<int> ps, pp;
   for (auto &c : ctx->ch) {
     const Dataset &d = ctx->ds[c.dataset];
-    const int P = d.P * 2 + (c.dev.model != 1), PS = d.P * 16 + d.S;
+    const int P = d.P * 4 + (c.dev.model != 1) * 2 + (c.dev.wm_update != 0);
+    const int PS = d.P * 16 + d.S;
     if (std::find(ps.begin(), ps.end(), P) == ps.end()) ps.push_back(P);
     if (c.pred_on && std::find(pp.begin(), pp.end(), PS) == pp.end()) pp.push_back(PS);
   }

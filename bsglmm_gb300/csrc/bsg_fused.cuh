@@ -41,7 +41,9 @@ constexpr int fused_min_blocks() {
 // covarGPU.cu:398-513): Z_iv ~ N(mu, 1/phi_iv) truncated by Y, then
 // phi_iv | Z, beta ~ Gamma((nu + 1) / 2, rate (nu + (Z - mu)^2) / 2), and the
 // coefficient draw uses X' Phi X and X' Phi (Z - b_WM WM).
-template <int P, int LPV, bool SUPP, bool MIX = false>
+// WMU: chains that draw beta_WM (one lane per voxel) also carry each voxel's
+// term of its conditional mean through the block partials.
+template <int P, int LPV, bool SUPP, bool MIX = false, bool WMU = false>
 __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
     fused_colour_kernel(const DatasetDev *__restrict__ dsv,
                         ChainDev *__restrict__ chv,
@@ -359,7 +361,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
     // ---- beta_WM | Z, beta (betaMGPU, covarGPU.cu:585-640): this voxel's
     // WM_v * sum_i (Z_iv - x_i' beta_v) with the new beta_v; with X c = 1,
     // sum_i (Z_iv - bwm) = c' acc.
-    if (ch.wm_update) {
+    if constexpr (WMU) {
       double sz = 0.0, sxb = 0.0;
 #pragma unroll
       for (int p = 0; p < P; ++p) {
@@ -428,8 +430,9 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
   __shared__ int is_last;
   const int lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
   constexpr int kColOff = kMaxPairs;
+  constexpr int NV = NT + P + (WMU ? 1 : 0);  // values reduced per block
 #pragma unroll
-  for (int q = 0; q <= NT + P; ++q) {
+  for (int q = 0; q < NV; ++q) {
     if (colour == 0 && q < NT) continue;
     double val = q < NT ? (double)pv[q] : (q < NT + P ? (double)bnew[q - NT] : wmt);
 #pragma unroll
@@ -441,7 +444,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
   const int vpb = blockDim.x / LPV;
   const int lb = bm.start / vpb;
   if (colour == 0) {
-    if (tid < P || tid == kMaxP) {
+    if (tid < P || (WMU && tid == kMaxP)) {
       const int q = tid < P ? kColOff + tid : kWmOff;
       double s = 0.0;
       for (int w = 0; w < nwarp; ++w) s += red[w][q];
@@ -461,7 +464,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
   }
   if (tid < kFusedVals) {
     const bool live =
-        tid < kMaxPairs ? tid < NT : (tid == kWmOff || (tid - kColOff) < P);
+        tid < kMaxPairs ? tid < NT : ((WMU && tid == kWmOff) || (tid - kColOff) < P);
     double s = 0.0;
     if (live)
       for (int w = 0; w < nwarp; ++w) s += red[w][tid];
@@ -482,7 +485,8 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
   const int n0 = d.n[0];
   const int nblk0 = (n0 + vpb - 1) / vpb;
   for (int q = warp; q < kFusedVals; q += nwarp) {
-    const bool live = q < kMaxPairs ? q < NT : (q == kWmOff || (q - kColOff) < P);
+    const bool live =
+        q < kMaxPairs ? q < NT : ((WMU && q == kWmOff) || (q - kColOff) < P);
     double s = 0.0;
     if (live) {
       for (int bb = lane; bb < nblk1; bb += 32)
@@ -506,7 +510,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
 // programmatic-stream-serialization attribute, so it may start once every
 // block of the previous kernel in the stream has passed its dependency
 // point.
-template <int P, int LPV, bool SUPP, bool MIX = false>
+template <int P, int LPV, bool SUPP, bool MIX = false, bool WMU = false>
 cudaError_t launch_one(int nblocks, int threads, cudaStream_t st, bool pdl,
                        const DatasetDev *ds, ChainDev *ch, const BlockMap *map,
                        int colour, const Supplied &sup) {
@@ -520,8 +524,8 @@ cudaError_t launch_one(int nblocks, int threads, cudaStream_t st, bool pdl,
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = pdl ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, fused_colour_kernel<P, LPV, SUPP, MIX>, ds, ch, map,
-                            colour, sup);
+  return cudaLaunchKernelEx(&cfg, fused_colour_kernel<P, LPV, SUPP, MIX, WMU>, ds, ch,
+                            map, colour, sup);
 }
 
 // Instantiation helper used by bsg_fused_l*.cu.

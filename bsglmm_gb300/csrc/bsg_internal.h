@@ -135,6 +135,10 @@ cudaError_t launch_fused(int P, int lpv, int threads, bool supplied,
                          const BlockMap *map, int nblocks, int colour,
                          const Supplied &sup, cudaStream_t st,
                          bool pdl = false);
+// The colour kernel of chains that draw beta_WM (one lane per voxel, Philox).
+cudaError_t launch_fused_wm(int P, int threads, const DatasetDev *ds, ChainDev *ch,
+                            const BlockMap *map, int nblocks, int colour,
+                            cudaStream_t st, bool pdl);
 // The colour kernel of the t/logit links (one lane per voxel, Philox).
 cudaError_t launch_fused_mix(int P, int threads, const DatasetDev *ds, ChainDev *ch,
                              const BlockMap *map, int nblocks, int colour,

@@ -491,6 +491,71 @@ def run_dic(args, rank, world, local):
         print(json.dumps(line))
 
 
+VARIANTS = {
+    "logit": "brain-sized study with the logistic link (t_8 scale mixture, "
+             "logit_factor 0.634): 91x109x91 grid, N=1000, P=5",
+    "t": "brain-sized study with the t_3 link (scale mixture of normals): "
+         "91x109x91 grid, N=1000, P=5",
+    "wm": "brain-sized study with a voxelwise WM map and the beta_WM update: "
+          "91x109x91 grid, N=1000, P=5",
+}
+
+
+def run_variant(args, rank, world, local):
+    """One sweep of the brain-sized study on a model variant (the logistic
+    link, or the beta_WM update), device time per sweep with L2 flushed,
+    against the plain probit sweep of the same study in the same process."""
+    import torch
+    import bsglmm_gb300 as bsg
+    from bsglmm_gb300 import synth
+    torch.cuda.set_device(local)
+    study = synth.config1(seed=1)
+    N, P, S, V = study.N, study.P, study.nsubtypes, study.V
+    flushbuf = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+    wm = (np.random.default_rng(7).random(V).astype(np.float32)
+          if args.workload == "wm" else None)
+
+    def timed(setup):
+        with bsg.Sampler(local) as s:
+            ds = s.add_dataset(study.mask, study.covar, study.data, S, wm)
+            ch = s.add_chain(ds, seed=chain_seed(rank), burnin=0, thin=1)
+            setup(s, ch)
+            for _ in range(args.warmup):
+                s.run_timed(1)
+            s.sync()
+            ms = []
+            for _ in range(args.steps):
+                flush_l2(flushbuf)
+                torch.cuda.synchronize()
+                ms.append(s.run_timed(1))
+            s.sync()
+            prof, nl = s.profile(min(args.steps, 20))
+            return float(np.median(ms)), prof[0] / nl[0], prof[1] / nl[1], s.launches_per_sweep()
+
+    with Clocks(local) as clk:
+        base = timed(lambda s, ch: None)
+        if args.workload in ("logit", "t"):
+            link = "logistic" if args.workload == "logit" else "t"
+            var = timed(lambda s, ch: s.set_model(ch, link))
+        else:
+            var = timed(lambda s, ch: s.set_wm_update(ch, True))
+    line = {
+        "metric": "subject-voxel updates/s of one sweep (model variant)",
+        "value": N * V / (var[0] * 1e-3), "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": var[0],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (f64 Omega/accumulators)", "data": "synthetic",
+        "config": {"workload": VARIANTS[args.workload], "V": V, "N": N, "P": P, "S": S,
+                   "l2": "flushed between timed sweeps", "timing": "device, median"},
+        "colour_kernel_ms": [var[1], var[2]], "gpu_launches_per_sweep": var[3],
+        "probit_same_study": {"ms_per_step": base[0], "value": N * V / (base[0] * 1e-3),
+                              "colour_kernel_ms": [base[1], base[2]]},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -501,11 +566,14 @@ def main():
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="brain",
-                    choices=["brain", "dic"] + sorted(BATCHED))
+                    choices=["brain", "dic"] + sorted(VARIANTS) + sorted(BATCHED))
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.workload == "dic" and args.impl == "ours":
         run_dic(args, rank, world, local)
+        return
+    if args.workload in VARIANTS and args.impl == "ours":
+        run_variant(args, rank, world, local)
         return
     if args.workload != "brain" and args.impl == "ours":
         run_batched(args, rank, world, local)

@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
       // flip by ymask = Y << 31); t ~ N(0,1) on (a, inf);
       // Z - bwm = x'beta + (Y ? t : -t); acc += x (Z - bwm).
       auto subject = [&](int col, uint32_t ymask, uint32_t kk, uint32_t isub,
-                         uint32_t gn, uint32_t gu) {
+                         uint32_t gn, uint32_t gu, float ph) {
         float x[P];
         const float4 v0 = *reinterpret_cast<const float4 *>(&Xs[col][0]);
         x[0] = v0.x;
@@ -133,7 +133,6 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
           // standardised: (Z - mu) sqrt(phi) ~ N(0, 1) on (a, inf) after the
           // outcome's sign flip, a = -/+ mu sqrt(phi)
           float *pp = ch.phi[colour] + (size_t)isub * nc + j;
-          const float ph = *pp;
           const float sd = rsqrt_approx(ph);
           const float a = __uint_as_float(__float_as_uint((m0 + bwm) * (ph * sd)) ^ ymask);
           float t = tn_lower_inv(fminf(a, kATail), kk);
@@ -143,9 +142,13 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
           const float r = __uint_as_float(__float_as_uint(t * sd) ^ ymask ^ 0x80000000u);
           const float zr = m0 + r;  // Z - b_WM WM
           float gm;
-          if (!gamma_mt_try(ch.mix_d, ch.mix_c, gn, gu, &gm))
+          if (ch.t_df == 3.f) {
+            // Gamma(2, 1) = Exp(1) + Exp(1) = -ln(u1 u2), exactly (t link)
+            gm = lg2_approx(u_of(gn) * u_of(gu)) * -0.693147181f;
+          } else if (!gamma_mt_try(ch.mix_d, ch.mix_c, gn, gu, &gm)) {
             gm = gamma_mt_more(ch.mix_d, ch.mix_c, isub, (uint32_t)v, sweep,
                                cid | kTagPhiMore, ch.key0, ch.key1, &ok);
+          }
           const float phn = 2.f * gm / fmaf(r, r, ch.t_df);
           *pp = phn;
           const float wz = phn * zr;
@@ -195,10 +198,23 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
           if (!MIX) return make_uint4(0, 0, 0, 0);
           return philox(make_uint4(i >> 1, (uint32_t)v, sweep, cid | kTagPhi), key);
         };
+        // MIX: the weights phi of a group of four subjects are loaded one
+        // group ahead (the stores of the current group may alias as far as
+        // the compiler knows, so it would not hoist them itself)
+        const float *phb = MIX ? ch.phi[colour] + j : nullptr;
         if (nbits == 32) {
+          float phc[4] = {1.f, 1.f, 1.f, 1.f}, phx[4] = {1.f, 1.f, 1.f, 1.f};
+          if (MIX) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) phc[q] = phb[(size_t)(i00 + q) * nc];
+          }
 #pragma unroll 1
           for (int b = 0; b < 32; b += 4) {
             const uint32_t i = i00 + (uint32_t)b;
+            if (MIX && b + 4 < 32) {
+#pragma unroll
+              for (int q = 0; q < 4; ++q) phx[q] = phb[(size_t)(i + 4 + q) * nc];
+            }
             uint4 r = make_uint4(0, 0, 0, 0);
             if (!SUPP) r = philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key);
             const uint4 g0 = gpair(i), g1 = gpair(i + 2);
@@ -206,8 +222,12 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
             for (int q = 0; q < 4; ++q) {
               const uint4 gq = q < 2 ? g0 : g1;
               subject(xo + b + q, yw << 31, variate(r, q, i + q), i + q,
-                      (q & 1) ? gq.z : gq.x, (q & 1) ? gq.w : gq.y);
+                      (q & 1) ? gq.z : gq.x, (q & 1) ? gq.w : gq.y, phc[q]);
               yw >>= 1;
+            }
+            if (MIX) {
+#pragma unroll
+              for (int q = 0; q < 4; ++q) phc[q] = phx[q];
             }
           }
         } else {
@@ -221,7 +241,8 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
               const uint4 gq = q < 2 ? g0 : g1;
               if (b + q < nbits)
                 subject(xo + b + q, yw << 31, variate(r, q, i + q), i + q,
-                        (q & 1) ? gq.z : gq.x, (q & 1) ? gq.w : gq.y);
+                        (q & 1) ? gq.z : gq.x, (q & 1) ? gq.w : gq.y,
+                        MIX ? phb[(size_t)(i + q) * nc] : 1.f);
               yw >>= 1;
             }
           }

@@ -689,12 +689,15 @@ static int mt_try(double d, double c, uint32_t kn, uint32_t ku, double *g) {
 /* phi | Z, beta ~ Gamma((nu + 1) / 2, rate (nu + r^2) / 2) for subject i of
  * voxel v: attempt 0 from counter (i / 2, v, sweep, PHI) (normal, uniform
  * in the first or second pair of words), further attempt pairs from
- * (i * 32 + q, v, sweep, PHI_MORE). */
+ * (i * 32 + q, v, sweep, PHI_MORE).  For alpha = 2 (the t link, nu = 3) the
+ * same pair of words gives -ln(u1 u2), a sum of two Exp(1). */
 static double mix_gamma(const orc_chain_cfg *cfg, double d, double c, uint32_t i,
                         uint32_t v, uint32_t sw, int *err) {
   uint32_t o[4];
   double g;
   philox(i >> 1, v, sw, (cfg->chain << 8) | ORC_TAG_PHI, cfg->key0, cfg->key1, o);
+  if (fabs(d - (2.0 - 1.0 / 3.0)) < 1e-12) /* alpha = 2: -ln(u1 u2), exactly */
+    return -log(orc_u_from_bits(o[(i & 1) * 2]) * orc_u_from_bits(o[(i & 1) * 2 + 1]));
   if (mt_try(d, c, o[(i & 1) * 2], o[(i & 1) * 2 + 1], &g)) return g;
   for (int q = 0; q < (ORC_GAMMA_MAX - 1) / 2; ++q) {
     philox(i * 32u + (uint32_t)q, v, sw, (cfg->chain << 8) | ORC_TAG_PHI_MORE,

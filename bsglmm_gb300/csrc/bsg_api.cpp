@@ -279,7 +279,9 @@ bsg_status build_plan(bsg_ctx *ctx) {
     CK(e);
   }
   const int vpb = ctx->threads / ctx->lpv;
-  bsg_status ps = ensure_partials(ctx, std::min(vpb, kParityThreads));
+  // partial rows for the smallest tile any kernel of this context uses
+  bsg_status ps =
+      ensure_partials(ctx, std::min({vpb, kParityThreads, ctx->threads / kMixLpv}));
   if (ps) return ps;
   std::vector<DatasetDev> hds;
   for (auto &d : ctx->ds) hds.push_back(d.dev);
@@ -311,8 +313,8 @@ bsg_status build_plan(bsg_ctx *ctx) {
       g->mix = mix;
       g->wm_any = wmu;
     }
-    // the t/logit and beta_WM kernels run one lane per voxel
-    const int gvpb = (mix || wmu) ? ctx->threads : vpb;
+    // the t/logit kernel runs kMixLpv lanes per voxel, the beta_WM one one
+    const int gvpb = mix ? ctx->threads / kMixLpv : (wmu ? ctx->threads : vpb);
     for (int c = 0; c < 2; ++c) map_chain(g->map[c], (int)ci, (int)d.vox[c].size(), gvpb, c);
     if (ctx->ch[ci].pred_on) {
       const ChainDev &cv = ctx->ch[ci].dev;

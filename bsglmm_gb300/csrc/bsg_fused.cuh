@@ -257,6 +257,13 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
 #pragma unroll
       for (int o = LPV / 2; o > 0; o >>= 1)
         acc[p] += __shfl_xor_sync(0xffffffffu, acc[p], o);
+    if constexpr (MIX) {
+#pragma unroll
+      for (int q = 0; q < NQ; ++q)
+#pragma unroll
+        for (int o = LPV / 2; o > 0; o >>= 1)
+          qw[q] += __shfl_xor_sync(0xffffffffu, qw[q], o);
+    }
   }
 
   // ---- dependency protocol (programmatic dependent launch) --------------

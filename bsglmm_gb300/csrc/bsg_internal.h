@@ -139,7 +139,8 @@ cudaError_t launch_fused(int P, int lpv, int threads, bool supplied,
 cudaError_t launch_fused_wm(int P, int threads, const DatasetDev *ds, ChainDev *ch,
                             const BlockMap *map, int nblocks, int colour,
                             cudaStream_t st, bool pdl);
-// The colour kernel of the t/logit links (one lane per voxel, Philox).
+// The colour kernel of the t/logit links (kMixLpv lanes per voxel, Philox).
+constexpr int kMixLpv = 2;
 cudaError_t launch_fused_mix(int P, int threads, const DatasetDev *ds, ChainDev *ch,
                              const BlockMap *map, int nblocks, int colour,
                              cudaStream_t st, bool pdl);

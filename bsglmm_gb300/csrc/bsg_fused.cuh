@@ -181,6 +181,60 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
 #pragma unroll
         for (int p = 0; p < P; ++p) acc[p] = fmaf(x[p], zr, acc[p]);
       };
+      // Probit with Philox variates, four subjects of one Philox call: the
+      // four inversion draws carry no control flow (so their dependency
+      // chains interleave), one vote per group sends the rare subjects
+      // beyond kATail to the bounded rejection sampler, then X'(Z - bwm)
+      // takes the four in order.  The same arithmetic as `subject`.
+      auto group4 = [&](int col0, uint32_t yw4, uint4 r, uint32_t i) {
+        float m0q[4], aq[4], zq[4];
+        auto row = [&](int col, float (&x)[P]) {
+          const float4 v0 = *reinterpret_cast<const float4 *>(&Xs[col][0]);
+          x[0] = v0.x;
+          if (P > 1) x[1] = v0.y;
+          if (P > 2) x[2] = v0.z;
+          if (P > 3) x[3] = v0.w;
+          if (P > 4) {
+            const float4 v1 = *reinterpret_cast<const float4 *>(&Xs[col][4]);
+            x[4] = v1.x;
+            if (P > 5) x[5] = v1.y;
+            if (P > 6) x[6] = v1.z;
+            if (P > 7) x[7] = v1.w;
+          }
+        };
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          float x[P];
+          row(col0 + q, x);
+          float m0 = 0.f;
+#pragma unroll
+          for (int p = 0; p < P; ++p) m0 = fmaf(beta[p], x[p], m0);
+          const uint32_t ym = (yw4 >> q) << 31;
+          const float a = __uint_as_float(__float_as_uint(m0 + bwm) ^ ym);
+          const float t = tn_lower_inv(fminf(a, kATail), pick4(r, q));
+          m0q[q] = m0;
+          aq[q] = a;
+          zq[q] = m0 + __uint_as_float(__float_as_uint(t) ^ ym ^ 0x80000000u);
+        }
+        const bool far = fmaxf(fmaxf(aq[0], aq[1]), fmaxf(aq[2], aq[3])) > kATail;
+        if (__any_sync(__activemask(), far)) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (aq[q] > kATail) {
+              const uint32_t ym = (yw4 >> q) << 31;
+              const float t = tn_lower_tail(aq[q], i + q, (uint32_t)v, sweep,
+                                            cid | kTagZTail, ch.key0, ch.key1, &ok);
+              zq[q] = m0q[q] + __uint_as_float(__float_as_uint(t) ^ ym ^ 0x80000000u);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          float x[P];
+          row(col0 + q, x);
+#pragma unroll
+          for (int p = 0; p < P; ++p) acc[p] = fmaf(x[p], zq[q], acc[p]);
+        }
+      };
       auto variate = [&](uint4 r, int q, uint32_t isub) -> uint32_t {
         if (SUPP) return __ldg(sup.ubits + (size_t)isub * d.V + v);
         return pick4(r, q);
@@ -217,13 +271,21 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
             }
             uint4 r = make_uint4(0, 0, 0, 0);
             if (!SUPP) r = philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key);
-            const uint4 g0 = gpair(i), g1 = gpair(i + 2);
+#ifndef BSG_SUBJECT_VOTE
+            if constexpr (!MIX && !SUPP) {
+              group4(xo + b, yw, r, i);
+              yw >>= 4;
+            } else
+#endif
+            {
+              const uint4 g0 = gpair(i), g1 = gpair(i + 2);
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              const uint4 gq = q < 2 ? g0 : g1;
-              subject(xo + b + q, yw << 31, variate(r, q, i + q), i + q,
-                      (q & 1) ? gq.z : gq.x, (q & 1) ? gq.w : gq.y, phc[q]);
-              yw >>= 1;
+              for (int q = 0; q < 4; ++q) {
+                const uint4 gq = q < 2 ? g0 : g1;
+                subject(xo + b + q, yw << 31, variate(r, q, i + q), i + q,
+                        (q & 1) ? gq.z : gq.x, (q & 1) ? gq.w : gq.y, phc[q]);
+                yw >>= 1;
+              }
             }
             if (MIX) {
 #pragma unroll

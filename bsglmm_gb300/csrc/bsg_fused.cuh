@@ -297,6 +297,13 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
             const uint32_t i = i00 + (uint32_t)b;
             uint4 r = make_uint4(0, 0, 0, 0);
             if (!SUPP) r = philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key);
+            if constexpr (!MIX && !SUPP) {
+              if (b + 4 <= nbits) {  // a whole group of the last word
+                group4(xo + b, yw, r, i);
+                yw >>= 4;
+                continue;
+              }
+            }
             const uint4 g0 = gpair(i), g1 = gpair(i + 2);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {

@@ -577,23 +577,29 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
   __syncthreads();
   if (!is_last) return;
   __threadfence();
-  // Sum the partial rows in block order (fixed, so the draw is bitwise
-  // reproducible): warp w takes values q = w, w + nwarp, ...
+  // Sum the partial rows in a fixed order (so the draw is bitwise
+  // reproducible): warp w takes the live values m = w, w + nwarp, ...; lane
+  // l the rows l, l + 32, ..., in four interleaved sums so that four loads
+  // are in flight, combined in a fixed order and then across lanes.
   const int n0 = d.n[0];
   const int nblk0 = (n0 + vpb - 1) / vpb;
-  for (int q = warp; q < kFusedVals; q += nwarp) {
-    const bool live =
-        q < kMaxPairs ? q < NT : ((WMU && q == kWmOff) || (q - kColOff) < P);
-    double s = 0.0;
-    if (live) {
-      for (int bb = lane; bb < nblk1; bb += 32)
-        s += __ldcg(ch.partials1 + (size_t)bb * kFusedVals + q);
-      if (q >= kColOff) {
-        const int q0 = q == kWmOff ? kMaxP : q - kColOff;
-        for (int bb = lane; bb < nblk0; bb += 32)
-          s += __ldcg(ch.partials0 + (size_t)bb * kP0Vals + q0);
-      }
+  auto rows = [&](const double *base, int stride, int nrow) -> double {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int bb = lane;
+    for (; bb + 96 < nrow; bb += 128) {
+      s0 += __ldcg(base + (size_t)bb * stride);
+      s1 += __ldcg(base + (size_t)(bb + 32) * stride);
+      s2 += __ldcg(base + (size_t)(bb + 64) * stride);
+      s3 += __ldcg(base + (size_t)(bb + 96) * stride);
     }
+    for (; bb < nrow; bb += 32) s0 += __ldcg(base + (size_t)bb * stride);
+    return (s0 + s1) + (s2 + s3);
+  };
+  for (int m = warp; m < NV; m += nwarp) {
+    const int q = m < NT ? m : (m < NT + P ? kColOff + (m - NT) : kWmOff);
+    double s = rows(ch.partials1 + q, kFusedVals, nblk1);
+    if (q >= kColOff)
+      s += rows(ch.partials0 + (q == kWmOff ? kMaxP : q - kColOff), kP0Vals, nblk0);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if (lane == 0) tot[q] = s;

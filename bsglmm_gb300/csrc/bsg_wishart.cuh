@@ -31,36 +31,19 @@ static __device__ double gamma_mt(double a, uint32_t slot, uint32_t sweep,
   return dd;
 }
 
-// In-place Cholesky of the lower triangle of the P x P matrix A (row-major
-// A[r*kMaxP + c]) by one warp, rows across lanes (the outer-product scheme
-// of cholesky.cpp:13-33).  Returns false (warp-uniform) on a non-positive
-// pivot.
-static __device__ bool chol_warp(double (*A)[kMaxP], int P, int lane) {
-  bool ok = true;
-  for (int k = 0; k < P; ++k) {
-    const double d = A[k][k];
-    ok = ok && (d > 0.0);
-    const double s = sqrt(d);
-    __syncwarp();
-    if (lane == k) A[k][k] = s;
-    if (lane > k && lane < P) A[lane][k] /= s;
-    __syncwarp();
-    if (lane > k && lane < P)
-      for (int j = k + 1; j <= lane; ++j) A[lane][j] -= A[lane][k] * A[j][k];
-    __syncwarp();
-  }
-  return ok;
-}
-
 // Omega | beta ~ Wishart(df, (S + I)^-1) by the Bartlett construction of
-// rwishart2 (cholesky.cpp:245-286) after chol -> invert -> chol
-// (covar.cpp:286-291, covarGPU.cu:1099-1104), FP64, one warp.
+// rwishart2 (cholesky.cpp:245-286), FP64, one warp.  The reference forms
+// chol((S + I)^-1) by chol -> invert -> chol (covar.cpp:286-291,
+// covarGPU.cu:1099-1104); the same factor is reached here with a third of
+// the dependent work: with the reverse (upper) Cholesky S + I = U U', the
+// inverse is U^-T U^-1 and U^-T is lower triangular with a positive
+// diagonal, so chol((S + I)^-1) = U^-T (the Cholesky factor is unique).
 static __device__ void wishart_warp(const ChainDev &ch, const DatasetDev &d,
                                     const double *tot, long long sweep,
                                     bool kept, long long nk, int supplied,
                                     const Supplied &sup, int lane) {
   __shared__ double A[kMaxP][kMaxP], Ai[kMaxP][kMaxP], T[kMaxP][kMaxP],
-      B[kMaxP][kMaxP];
+      B[kMaxP][kMaxP], rd[kMaxP];
   const int P = d.P;
   const uint32_t cid = ch.chain_id << 8, sw = (uint32_t)sweep;
   int err = 0;
@@ -71,26 +54,40 @@ static __device__ void wishart_warp(const ChainDev &ch, const DatasetDev &d,
       T[r][c] = 0.0;
     }
   __syncwarp();
-  bool ok = chol_warp(A, P, lane);
-  if (ok) {
-    // column `lane` of (G G')^-1 by forward then back substitution
-    if (lane < P) {
-      double col[kMaxP];
-      for (int i = 0; i < P; ++i) col[i] = (i == lane) ? 1.0 : 0.0;
-      for (int i = 0; i < P; ++i) {
-        double s = 0.0;
-        for (int j = 0; j < i; ++j) s += A[i][j] * col[j];
-        col[i] = (col[i] - s) / A[i][i];
-      }
-      for (int i = P - 1; i >= 0; --i) {
-        double s = 0.0;
-        for (int j = i + 1; j < P; ++j) s += A[j][i] * col[j];
-        col[i] = (col[i] - s) / A[i][i];
-      }
-      for (int i = 0; i < P; ++i) Ai[lane][i] = col[i];  // row `lane` of Ai
+  // S + I = U U' with U upper, last pivot first; U goes to the upper
+  // triangle of A (diagonal included), the lower triangle holds the
+  // remaining leading block, rd[k] = 1 / U[k][k].
+  bool ok = true;
+  for (int k = P - 1; k >= 0; --k) {
+    const double dk = A[k][k];
+    ok = ok && (dk > 0.0);
+    const double rs = rsqrt(dk);
+    __syncwarp();
+    if (lane < k) A[lane][k] = A[k][lane] * rs;
+    if (lane == k) {
+      A[k][k] = dk * rs;
+      rd[k] = rs;
     }
     __syncwarp();
-    ok = chol_warp(Ai, P, lane);
+    if (lane < k)
+      for (int j = 0; j <= lane; ++j) A[lane][j] -= A[lane][k] * A[j][k];
+    __syncwarp();
+  }
+  if (ok) {
+    // column `lane` of W = U^-1 (upper): W[i][j] = -rd[i] sum_{k>i} U[i][k] W[k][j];
+    // the factor L = U^-T = W' goes to Ai (lower)
+    if (lane < P) {
+      const int j = lane;
+      double w[kMaxP];
+      w[j] = rd[j];
+      for (int i = j - 1; i >= 0; --i) {
+        double s = 0.0;
+        for (int k = i + 1; k <= j; ++k) s += A[i][k] * w[k];
+        w[i] = -rd[i] * s;
+      }
+      for (int i = 0; i < P; ++i) Ai[j][i] = i <= j ? w[i] : 0.0;
+    }
+    __syncwarp();
   }
   if (ok) {
     const double df = (double)d.V + (double)ch.df_offset;

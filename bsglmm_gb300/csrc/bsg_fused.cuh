@@ -271,13 +271,10 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
             }
             uint4 r = make_uint4(0, 0, 0, 0);
             if (!SUPP) r = philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key);
-#ifndef BSG_SUBJECT_VOTE
             if constexpr (!MIX && !SUPP) {
               group4(xo + b, yw, r, i);
               yw >>= 4;
-            } else
-#endif
-            {
+            } else {
               const uint4 g0 = gpair(i), g1 = gpair(i + 2);
 #pragma unroll
               for (int q = 0; q < 4; ++q) {

@@ -235,6 +235,93 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
           for (int p = 0; p < P; ++p) acc[p] = fmaf(x[p], zq[q], acc[p]);
         }
       };
+      // The t/logit links, four subjects: Z by inversion and the first
+      // Marsaglia-Tsang attempt for all four without control flow, one vote
+      // for the rare tail draws and gamma retries, then phi, X' Phi (Z - bwm)
+      // and X' Phi X for the four in order.  The same arithmetic as `subject`.
+      auto group4_mix = [&](int col0, uint32_t yw4, uint4 r, uint32_t i, uint4 g0,
+                            uint4 g1, const float (&ph4)[4]) {
+        float m0q[4], aq[4], sdq[4], rq[4], gq[4];
+        bool bad[4];
+        auto row = [&](int col, float (&x)[P]) {
+          const float4 v0 = *reinterpret_cast<const float4 *>(&Xs[col][0]);
+          x[0] = v0.x;
+          if (P > 1) x[1] = v0.y;
+          if (P > 2) x[2] = v0.z;
+          if (P > 3) x[3] = v0.w;
+          if (P > 4) {
+            const float4 v1 = *reinterpret_cast<const float4 *>(&Xs[col][4]);
+            x[4] = v1.x;
+            if (P > 5) x[5] = v1.y;
+            if (P > 6) x[6] = v1.z;
+            if (P > 7) x[7] = v1.w;
+          }
+        };
+        const bool t3 = ch.t_df == 3.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          float x[P];
+          row(col0 + q, x);
+          float m0 = 0.f;
+#pragma unroll
+          for (int p = 0; p < P; ++p) m0 = fmaf(beta[p], x[p], m0);
+          const uint32_t ym = (yw4 >> q) << 31;
+          const float ph = ph4[q];
+          const float sd = rsqrt_approx(ph);
+          const float a = __uint_as_float(__float_as_uint((m0 + bwm) * (ph * sd)) ^ ym);
+          const float t = tn_lower_inv(fminf(a, kATail), pick4(r, q));
+          m0q[q] = m0;
+          aq[q] = a;
+          sdq[q] = sd;
+          rq[q] = __uint_as_float(__float_as_uint(t * sd) ^ ym ^ 0x80000000u);
+          const uint4 gg = q < 2 ? g0 : g1;
+          const uint32_t gn = (q & 1) ? gg.z : gg.x, gu = (q & 1) ? gg.w : gg.y;
+          float g;
+          if (t3) {
+            g = lg2_approx(u_of(gn) * u_of(gu)) * -0.693147181f;
+            bad[q] = false;
+          } else {
+            bad[q] = !gamma_mt_try(ch.mix_d, ch.mix_c, gn, gu, &g);
+          }
+          gq[q] = g;
+        }
+        const bool rare = (fmaxf(fmaxf(aq[0], aq[1]), fmaxf(aq[2], aq[3])) > kATail) |
+                          bad[0] | bad[1] | bad[2] | bad[3];
+        if (__any_sync(__activemask(), rare)) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            if (aq[q] > kATail) {
+              const uint32_t ym = (yw4 >> q) << 31;
+              const float t = tn_lower_tail(aq[q], i + q, (uint32_t)v, sweep,
+                                            cid | kTagZTail, ch.key0, ch.key1, &ok);
+              rq[q] = __uint_as_float(__float_as_uint(t * sdq[q]) ^ ym ^ 0x80000000u);
+            }
+            if (bad[q])
+              gq[q] = gamma_mt_more(ch.mix_d, ch.mix_c, i + q, (uint32_t)v, sweep,
+                                    cid | kTagPhiMore, ch.key0, ch.key1, &ok);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          float x[P];
+          row(col0 + q, x);
+          const float phn = 2.f * gq[q] / fmaf(rq[q], rq[q], ch.t_df);
+          ch.phi[colour][(size_t)(i + q) * nc + j] = phn;
+          const float wz = phn * (m0q[q] + rq[q]);
+          float px[P];
+#pragma unroll
+          for (int p = 0; p < P; ++p) {
+            acc[p] = fmaf(x[p], wz, acc[p]);
+            px[p] = phn * x[p];
+          }
+#pragma unroll
+          for (int a2 = 0; a2 < P; ++a2)
+#pragma unroll
+            for (int b2 = 0; b2 <= a2; ++b2)
+              qw[tri(a2, b2) < NQ ? tri(a2, b2) : 0] =
+                  fmaf(px[a2], x[b2], qw[tri(a2, b2) < NQ ? tri(a2, b2) : 0]);
+        }
+      };
       auto variate = [&](uint4 r, int q, uint32_t isub) -> uint32_t {
         if (SUPP) return __ldg(sup.ubits + (size_t)isub * d.V + v);
         return pick4(r, q);
@@ -273,6 +360,9 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
             if (!SUPP) r = philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key);
             if constexpr (!MIX && !SUPP) {
               group4(xo + b, yw, r, i);
+              yw >>= 4;
+            } else if constexpr (MIX) {
+              group4_mix(xo + b, yw, r, i, gpair(i), gpair(i + 2), phc);
               yw >>= 4;
             } else {
               const uint4 g0 = gpair(i), g1 = gpair(i + 2);

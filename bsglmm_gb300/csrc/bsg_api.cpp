@@ -253,10 +253,15 @@ bsg_status ensure_partials(bsg_ctx *ctx, int vpb) {
   return BSG_OK;
 }
 
-// Block map of one colour for one chain: tiles of vpb voxels; colour 1
-// always has at least one block, whose last arrival draws Omega.
+// Block map of one colour for one chain: tiles of vpb voxels, at least one
+// block per colour even when the colour has no voxels.  Colour 1's last
+// arrival draws Omega; and the launch protocol relies on the colours
+// alternating (a colour kernel's early phase reads its own colour's state,
+// final once the other colour's kernel has passed its dependency point),
+// so neither colour's launch may be left out.
 void map_chain(std::vector<BlockMap> &m, int chain, int n, int vpb, int colour) {
-  if (n == 0 && colour == 1) m.push_back({(int32_t)chain, 0});
+  (void)colour;
+  if (n == 0) m.push_back({(int32_t)chain, 0});
   for (int s = 0; s < n; s += vpb) m.push_back({(int32_t)chain, (int32_t)s});
 }
 

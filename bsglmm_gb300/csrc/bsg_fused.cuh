@@ -637,7 +637,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
     }
     __syncthreads();
     if (tid == 0) {  // the last colour-0 block advances this colour's count
-      const int nblk0 = (nc + vpb - 1) / vpb;
+      const int nblk0 = max(1, (nc + vpb - 1) / vpb);
       if (atomicAdd(ch.done, 1u) == (unsigned)(nblk0 - 1)) {
         ch.sweep[0] = sweep_ll + 1;
         ch.done[0] = 0u;
@@ -669,7 +669,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
   // l the rows l, l + 32, ..., in four interleaved sums so that four loads
   // are in flight, combined in a fixed order and then across lanes.
   const int n0 = d.n[0];
-  const int nblk0 = (n0 + vpb - 1) / vpb;
+  const int nblk0 = max(1, (n0 + vpb - 1) / vpb);
   auto rows = [&](const double *base, int stride, int nrow) -> double {
     double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
     int bb = lane;

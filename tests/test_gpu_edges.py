@@ -1,0 +1,84 @@
+"""Edge shapes of the colour kernels against the FP64 oracle chain on the
+same counters: more subjects than one shared-memory chunk (512) with a
+partial last outcome word, a single subject, single-voxel masks (one colour
+empty), and several P at once in one context."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RTOL = ATOL = 1e-4
+
+
+def _study(seed, shape, N, P, S=1, fill=0.6, mask=None):
+    rng = np.random.default_rng(seed)
+    X, Y, Z = shape
+    if mask is None:
+        mask = (rng.random((Z, Y, X)) < fill).astype(np.uint8)
+    V = int(mask.sum())
+    covar = np.ones((P, N), np.float32)
+    if P > 1:
+        covar[1:] = rng.standard_normal((P - 1, N)).astype(np.float32)
+    eta = rng.normal(-0.5, 0.7, (N, V))
+    data = (rng.standard_normal((N, V)) < eta).astype(np.uint8)
+    return mask, covar, data, S
+
+
+def _compare(oracle_mod, mask, covar, data, S, seed, sweeps=2):
+    import bsglmm_gb300 as bsg
+    pb = oracle_mod.Problem(mask, covar, data, S)
+    with bsg.Sampler() as s:
+        ds = s.add_dataset(mask, covar, data, S)
+        ch = s.add_chain(ds, seed=seed)
+        s.run(1)
+        o = pb.chain(seed, 1)
+        assert np.allclose(s.beta(ch), o["beta"], rtol=RTOL, atol=ATOL)
+        assert np.allclose(s.omega(ch), o["omega"], rtol=RTOL,
+                           atol=ATOL * np.abs(o["omega"]).max())
+        if sweeps > 1:
+            s.run(sweeps - 1)
+            o = pb.chain(seed, sweeps - 1, s0=1, spatcoef=o["beta"], omega=o["omega"])
+            assert np.allclose(s.beta(ch), o["beta"], rtol=1e-3, atol=1e-3)
+        s.sync()
+
+
+@pytest.mark.parametrize("N", [600, 1025])
+def test_subjects_across_chunks_and_partial_word(oracle_mod, N):
+    """600 = 512 + 88 and 1025 = 2 x 512 + 1: two or three shared-memory
+    chunks, the last outcome word partial (24 and 1 subjects)."""
+    mask, covar, data, S = _study(3, (6, 6, 5), N, 3)
+    _compare(oracle_mod, mask, covar, data, S, seed=0xC0FFEE)
+
+
+def test_single_subject(oracle_mod):
+    mask, covar, data, S = _study(4, (7, 6, 5), 1, 1)
+    _compare(oracle_mod, mask, covar, data, S, seed=77)
+
+
+@pytest.mark.parametrize("pos", [(0, 0, 0), (0, 0, 1)])
+def test_single_voxel_mask(oracle_mod, pos):
+    """One in-mask voxel: only one colour has voxels (the other colour's
+    kernel has no work; the colour-1 kernel still draws Omega)."""
+    mask = np.zeros((4, 4, 4), np.uint8)
+    mask[pos] = 1
+    _, covar, data, S = _study(5, (4, 4, 4), 20, 2, mask=mask)
+    _compare(oracle_mod, mask, covar, data, S, seed=91, sweeps=3)
+
+
+def test_mixed_p_in_one_context(oracle_mod):
+    """Chains of P = 1, 4 and 8 in one context run as three launch groups on
+    parallel graph branches; each equals its own oracle chain."""
+    import bsglmm_gb300 as bsg
+    studies = [_study(10 + P, (6, 5, 5), 40 + P, P) for P in (1, 4, 8)]
+    seeds = [5, 6, 7]
+    with bsg.Sampler() as s:
+        chs = []
+        for (mask, covar, data, S), seed in zip(studies, seeds):
+            ds = s.add_dataset(mask, covar, data, S)
+            chs.append(s.add_chain(ds, seed=seed))
+        s.run(1)
+        for ch, (mask, covar, data, S), seed in zip(chs, studies, seeds):
+            o = oracle_mod.Problem(mask, covar, data, S).chain(seed, 1, chain_id=ch)
+            assert np.allclose(s.beta(ch), o["beta"], rtol=RTOL, atol=ATOL)

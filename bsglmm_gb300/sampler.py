@@ -315,16 +315,39 @@ class Sampler:
 
 def mcmc(mask, covar, data, ntypes: int = 1, maxiter: int = 100000,
          burnin: int = 50000, seed: int = 1, wm=None, beta_wm: float = 0.0,
-         df_offset: int | None = None, device: int = 0) -> dict:
+         df_offset: int | None = None, device: int = 0, model="probit",
+         wm_update: bool = False, predictive: bool = False) -> dict:
     """The reference's chain (mcmc.cpp:311-651): sweeps 0..MAXITER, kept
     iff iter > BURNIN and iter % SAVE_ITER == 0; returns the output maps
-    and the number of kept sweeps (TOTSAV)."""
+    and the number of kept sweeps (TOTSAV).
+
+    model: "probit", "logistic" or "t" (the reference's MODEL 1, 0, 2).
+    wm_update: draw beta_WM every sweep (the reference's WM argument); adds
+    "bWM" (the kept-sweep mean of beta_WM WM_v) and "beta_WM".
+    predictive: run the DIC/Qhat pass on kept sweeps; adds "DIC" (DE, ED,
+    PD, DIC) and "Qhat" (log scale, [N][ntypes])."""
     with Sampler(device) as s:
         ds = s.add_dataset(mask, covar, data, ntypes, wm)
         ch = s.add_chain(ds, seed=seed, burnin=burnin,
                          thin=save_iter_rule(maxiter, burnin),
                          df_offset=df_offset, beta_wm=beta_wm)
+        if model != "probit" and model != 1:
+            s.set_model(ch, model)
+        if wm_update:
+            s.set_wm_update(ch, True)
+        if predictive:
+            s.set_predictive(ch, True)
         s.run(maxiter + 1)
         out = s.maps(ch)
         out["TOTSAV"] = s.sweep_count(ch)[1]
+        if wm_update:
+            cur, mean = s.beta_wm(ch)
+            m = np.asarray(mask).astype(bool)
+            bwm = np.zeros(m.shape)
+            bwm[m] = mean * (np.ones(int(m.sum())) if wm is None
+                             else np.asarray(wm, dtype=np.float64))
+            out["bWM"], out["beta_WM"] = bwm, cur
+        if predictive and out["TOTSAV"] > 0:
+            out["DIC"] = s.dic(ch)
+            out["Qhat"] = s.predictive(ch)[0]
         return out

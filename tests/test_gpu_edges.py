@@ -82,3 +82,27 @@ def test_mixed_p_in_one_context(oracle_mod):
         for ch, (mask, covar, data, S), seed in zip(chs, studies, seeds):
             o = oracle_mod.Problem(mask, covar, data, S).chain(seed, 1, chain_id=ch)
             assert np.allclose(s.beta(ch), o["beta"], rtol=RTOL, atol=ATOL)
+
+
+def test_mcmc_convenience_equals_sampler():
+    """bsglmm_gb300.mcmc() with the WM update and the DIC pass equals the
+    same chain driven through Sampler."""
+    import bsglmm_gb300 as bsg
+    mask, covar, data, S = _study(21, (7, 6, 6), 30, 3)
+    V = int(mask.sum())
+    wm = np.random.default_rng(22).random(V).astype(np.float32)
+    out = bsg.mcmc(mask, covar, data, ntypes=1, maxiter=40, burnin=10, seed=9, wm=wm,
+                   wm_update=True, predictive=True)
+    with bsg.Sampler() as s:
+        ds = s.add_dataset(mask, covar, data, 1, wm)
+        ch = s.add_chain(ds, seed=9, burnin=10, thin=bsg.save_iter_rule(40, 10))
+        s.set_wm_update(ch, True)
+        s.set_predictive(ch, True)
+        s.run(41)
+        maps = s.maps(ch)
+        dic = s.dic(ch)
+        cur, mean = s.beta_wm(ch)
+    assert out["TOTSAV"] == 1
+    assert np.array_equal(out["spatCoef"], maps["spatCoef"])
+    assert out["DIC"] == dic and out["beta_WM"] == cur
+    assert np.array_equal(out["bWM"][mask.astype(bool)], mean * wm.astype(np.float64))

@@ -357,6 +357,33 @@ def batched_workload(name):
     raise ValueError(name)
 
 
+RHAT_BURNIN, RHAT_SWEEPS = 300, 200  # sweeps behind the c4 R-hat figure
+
+
+def cross_chain_rhat(s, nchains: int, burnin: int, sweeps: int) -> dict:
+    """Gelman-Rubin R-hat of every coefficient map entry across the chains
+    of one study, from each chain's posterior mean and variance over
+    `sweeps` sweeps after `burnin` more (the accumulators are reset in
+    between)."""
+    s.run(burnin)
+    for c in range(nchains):
+        s.reset_accumulators(c)
+    s.run(sweeps)
+    means, vars_ = [], []
+    for c in range(nchains):
+        m, v, _, n = s.posterior(c)
+        means.append(m)
+        vars_.append(v)
+    m = np.stack(means)
+    w = np.mean(np.stack(vars_), axis=0)
+    b = n * np.var(m, axis=0, ddof=1)
+    var_plus = (n - 1) / n * w + b / n
+    r = np.sqrt(var_plus / w).ravel()
+    return {"burnin": burnin, "sweeps": sweeps, "chains": nchains, "entries": int(r.size),
+            "median": float(np.median(r)), "p99": float(np.percentile(r, 99)),
+            "max": float(r.max())}
+
+
 def run_batched(args, rank, world, local):
     """Throughput of one context holding every chain of the workload (one
     batched launch per P group and colour) against the plain form: each
@@ -393,6 +420,9 @@ def run_batched(args, rank, world, local):
     with Clocks(local) as clk:
         t_b = timed([batched], args.steps)
     launches = batched.launches_per_sweep()
+    rhat = None
+    if args.workload == "c4":
+        rhat = cross_chain_rhat(batched, sum(nchains), RHAT_BURNIN, RHAT_SWEEPS)
     batched.close()
     plain = None
     if args.workload in ("c0", "c3"):
@@ -422,6 +452,7 @@ def run_batched(args, rank, world, local):
         "sweeps_per_s": 1.0 / t_b, "gpu_launches_per_sweep": launches,
         "plain": plain,
         "batched_over_plain": (upd / t_b) / plain["value"] if plain else None,
+        "rhat": rhat,
         "clocks": clk.summary(),
     }
     if rank == 0:
@@ -498,6 +529,8 @@ VARIANTS = {
          "91x109x91 grid, N=1000, P=5",
     "wm": "brain-sized study with a voxelwise WM map and the beta_WM update: "
           "91x109x91 grid, N=1000, P=5",
+    "c2": "precision form: the brain-sized mask with N=2000, P=8 (FP32 sweep, "
+          "FP64 Omega pair sums, Cholesky and accumulators), 1 chain",
 }
 
 
@@ -509,7 +542,7 @@ def run_variant(args, rank, world, local):
     import bsglmm_gb300 as bsg
     from bsglmm_gb300 import synth
     torch.cuda.set_device(local)
-    study = synth.config1(seed=1)
+    study = synth.config2() if args.workload == "c2" else synth.config1(seed=1)
     N, P, S, V = study.N, study.P, study.nsubtypes, study.V
     flushbuf = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
     wm = (np.random.default_rng(7).random(V).astype(np.float32)
@@ -537,8 +570,10 @@ def run_variant(args, rank, world, local):
         if args.workload in ("logit", "t"):
             link = "logistic" if args.workload == "logit" else "t"
             var = timed(lambda s, ch: s.set_model(ch, link))
-        else:
+        elif args.workload == "wm":
             var = timed(lambda s, ch: s.set_wm_update(ch, True))
+        else:  # c2: the plain sweep of its own study
+            var = base
     line = {
         "metric": "subject-voxel updates/s of one sweep (model variant)",
         "value": N * V / (var[0] * 1e-3), "unit": UNIT, "n_gpus": 1,

@@ -132,6 +132,29 @@ void *dalloc(bsg_ctx *ctx, size_t bytes, cudaError_t *e) {
   return p;
 }
 
+// Every copy and fill runs on the context stream, so that it is ordered with
+// the sweep kernels (the context stream is non-blocking: work on the legacy
+// default stream would race it).  A pageable host source is staged before
+// cudaMemcpyAsync returns; a page-locked one is read later by the copy
+// engine, so the copy is waited for before the caller may reuse the buffer.
+// A device-to-host copy is always waited for.
+cudaError_t h2d(bsg_ctx *ctx, void *dst, const void *src, size_t n) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, ctx->stream);
+  if (e != cudaSuccess) return e;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, src) != cudaSuccess) {
+    cudaGetLastError();
+    return cudaStreamSynchronize(ctx->stream);
+  }
+  return a.type == cudaMemoryTypeUnregistered ? cudaSuccess
+                                              : cudaStreamSynchronize(ctx->stream);
+}
+
+cudaError_t d2h(bsg_ctx *ctx, void *dst, const void *src, size_t n) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, ctx->stream);
+  return e != cudaSuccess ? e : cudaStreamSynchronize(ctx->stream);
+}
+
 void dfree(bsg_ctx *ctx, void *p) {
   if (!p) return;
   for (size_t i = 0; i < ctx->owned.size(); ++i)
@@ -202,7 +225,7 @@ template <typename T>
 T *upload(bsg_ctx *ctx, const T *host, size_t n, cudaError_t *e) {
   T *p = (T *)dalloc(ctx, sizeof(T) * n, e);
   if (!p) return nullptr;
-  if (n) *e = cudaMemcpy(p, host, sizeof(T) * n, cudaMemcpyHostToDevice);
+  if (n) *e = h2d(ctx, p, host, sizeof(T) * n);
   return *e == cudaSuccess ? p : nullptr;
 }
 
@@ -292,10 +315,8 @@ bsg_status build_plan(bsg_ctx *ctx) {
   for (auto &d : ctx->ds) hds.push_back(d.dev);
   std::vector<ChainDev> hch;
   for (auto &c : ctx->ch) hch.push_back(c.dev);
-  CK(cudaMemcpy(ctx->d_ds, hds.data(), sizeof(DatasetDev) * hds.size(),
-                cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(ctx->d_ch, hch.data(), sizeof(ChainDev) * hch.size(),
-                cudaMemcpyHostToDevice));
+  CK(h2d(ctx, ctx->d_ds, hds.data(), sizeof(DatasetDev) * hds.size()));
+  CK(h2d(ctx, ctx->d_ch, hch.data(), sizeof(ChainDev) * hch.size()));
   for (auto &g : ctx->groups) {
     for (int c = 0; c < 2; ++c) dfree(ctx, g.d_map[c]);
     for (auto &pr : g.pred) {
@@ -484,10 +505,10 @@ bsg_status ensure_pred(bsg_ctx *ctx, Chain &c) {
   CK(e);
   PredCounters *pc = (PredCounters *)dalloc(ctx, sizeof(PredCounters), &e);
   CK(e);
-  CK(cudaMemset(cv.mpred, 0, sizeof(double) * N * G));
-  CK(cudaMemset(cv.qhat, 0, sizeof(double) * N * G));
-  CK(cudaMemset(cv.pred_sums, 0, sizeof(double) * 2));
-  CK(cudaMemset(pc, 0, sizeof(PredCounters)));
+  CK(cudaMemsetAsync(cv.mpred, 0, sizeof(double) * N * G, ctx->stream));
+  CK(cudaMemsetAsync(cv.qhat, 0, sizeof(double) * N * G, ctx->stream));
+  CK(cudaMemsetAsync(cv.pred_sums, 0, sizeof(double) * 2, ctx->stream));
+  CK(cudaMemsetAsync(pc, 0, sizeof(PredCounters), ctx->stream));
   cv.npred = &pc->npred;
   cv.pred_done = &pc->done;
   cv.pred_tiles = T;
@@ -690,7 +711,7 @@ bsg_status bsg_add_dataset(bsg_ctx *ctx, const bsg_dataset_desc *desc,
   CK(e);
   int *status = (int *)dalloc(ctx, sizeof(int), &e);
   CK(e);
-  CK(cudaMemset(status, 0, sizeof(int)));
+  CK(cudaMemsetAsync(status, 0, sizeof(int), ctx->stream));
   const int sy = d.PX, sz = d.PX * d.PY;
   const int off[6] = {-1, 1, -sy, sy, -sz, sz};
   for (int c = 0; c < 2; ++c) {
@@ -722,7 +743,7 @@ bsg_status bsg_add_dataset(bsg_ctx *ctx, const bsg_dataset_desc *desc,
     CK(launch_pack(bytes, d.N, d.V, nc, dv.vidx[c], yb, status, ctx->stream));
   }
   int bad = 0;
-  CK(cudaMemcpyAsync(&bad, status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(d2h(ctx, &bad, status, sizeof(int)));
   CK(cudaStreamSynchronize(ctx->stream));
   dfree(ctx, bytes);
   dfree(ctx, status);
@@ -764,7 +785,7 @@ bsg_status bsg_add_chain(bsg_ctx *ctx, int32_t dataset_id,
   const int P = d.P;
   cv.beta = (float *)dalloc(ctx, sizeof(float) * (size_t)P * d.Vp, &e);
   CK(e);
-  CK(cudaMemset(cv.beta, 0, sizeof(float) * (size_t)P * d.Vp));
+  CK(cudaMemsetAsync(cv.beta, 0, sizeof(float) * (size_t)P * d.Vp, ctx->stream));
   std::vector<double> eye((size_t)P * P, 0.0);
   std::vector<float> eyef((size_t)P * P, 0.f);
   for (int i = 0; i < P; ++i) eye[i + i * P] = 1.0, eyef[i + i * P] = 1.f;
@@ -777,10 +798,10 @@ bsg_status bsg_add_chain(bsg_ctx *ctx, int32_t dataset_id,
   WmState *wst = (WmState *)dalloc(ctx, sizeof(WmState), &e);
   CK(e);
   const WmState w0{0.0, desc->beta_wm, 0};
-  CK(cudaMemcpy(wst, &w0, sizeof(w0), cudaMemcpyHostToDevice));
+  CK(h2d(ctx, wst, &w0, sizeof(w0)));
   cv.wm_sum = &wst->sum;
   cv.wm_beta = &wst->beta;
-  CK(cudaMemset(cv.colmean, 0, sizeof(float) * P));
+  CK(cudaMemsetAsync(cv.colmean, 0, sizeof(float) * P, ctx->stream));
   const size_t nacc = (size_t)P * d.V, nprb = (size_t)d.S * d.V;
   cv.acc_sum = (double *)dalloc(ctx, sizeof(double) * nacc, &e);
   CK(e);
@@ -788,12 +809,12 @@ bsg_status bsg_add_chain(bsg_ctx *ctx, int32_t dataset_id,
   CK(e);
   cv.prb_sum = (double *)dalloc(ctx, sizeof(double) * (nprb ? nprb : 1), &e);
   CK(e);
-  CK(cudaMemset(cv.acc_sum, 0, sizeof(double) * nacc));
-  CK(cudaMemset(cv.acc_sq, 0, sizeof(double) * nacc));
-  if (nprb) CK(cudaMemset(cv.prb_sum, 0, sizeof(double) * nprb));
+  CK(cudaMemsetAsync(cv.acc_sum, 0, sizeof(double) * nacc, ctx->stream));
+  CK(cudaMemsetAsync(cv.acc_sq, 0, sizeof(double) * nacc, ctx->stream));
+  if (nprb) CK(cudaMemsetAsync(cv.prb_sum, 0, sizeof(double) * nprb, ctx->stream));
   ChainCounters *cnt = (ChainCounters *)dalloc(ctx, sizeof(ChainCounters), &e);
   CK(e);
-  CK(cudaMemset(cnt, 0, sizeof(ChainCounters)));
+  CK(cudaMemsetAsync(cnt, 0, sizeof(ChainCounters), ctx->stream));
   cv.sweep = cnt->sweep;
   cv.nkept = &cnt->nkept;
   cv.done = cnt->done;
@@ -801,7 +822,7 @@ bsg_status bsg_add_chain(bsg_ctx *ctx, int32_t dataset_id,
   if (!ctx->any_status) {
     ctx->any_status = (int *)dalloc(ctx, sizeof(int), &e);
     CK(e);
-    CK(cudaMemset(ctx->any_status, 0, sizeof(int)));
+    CK(cudaMemsetAsync(ctx->any_status, 0, sizeof(int), ctx->stream));
   }
   cv.any_status = ctx->any_status;
   ctx->ch.push_back(c);
@@ -856,12 +877,12 @@ bsg_status bsg_sync(bsg_ctx *ctx) {
   CK(cudaStreamSynchronize(ctx->stream));
   int bits = 0;
   if (ctx->any_status)
-    CK(cudaMemcpy(&bits, ctx->any_status, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(d2h(ctx, &bits, ctx->any_status, sizeof(int)));
   if (bits) {
     ctx->err = "sampler:" + status_text(bits);
     for (size_t i = 0; i < ctx->ch.size(); ++i) {
       int b = 0;
-      CK(cudaMemcpy(&b, ctx->ch[i].dev.status, sizeof(int), cudaMemcpyDeviceToHost));
+      CK(d2h(ctx, &b, ctx->ch[i].dev.status, sizeof(int)));
       if (b) ctx->err += " (chain " + std::to_string(i) + ")";
     }
     return status_from_bits(bits);
@@ -982,7 +1003,7 @@ bsg_status bsg_get_beta(bsg_ctx *ctx, int32_t chain, float *out) {
   const Dataset &d = ctx->ds[c.dataset];
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
-  CK(cudaMemcpy(out, c.dev.beta, sizeof(float) * (size_t)d.P * d.Vp, cudaMemcpyDeviceToHost));
+  CK(d2h(ctx, out, c.dev.beta, sizeof(float) * (size_t)d.P * d.Vp));
   return BSG_OK;
 }
 
@@ -1001,7 +1022,7 @@ bsg_status bsg_set_beta(bsg_ctx *ctx, int32_t chain, const float *in) {
       if (!inmask[s]) b[(size_t)p * d.Vp + s] = 0.f;
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
-  CK(cudaMemcpy(c.dev.beta, b.data(), sizeof(float) * b.size(), cudaMemcpyHostToDevice));
+  CK(h2d(ctx, c.dev.beta, b.data(), sizeof(float) * b.size()));
   return BSG_OK;
 }
 
@@ -1011,7 +1032,7 @@ bsg_status bsg_get_omega(bsg_ctx *ctx, int32_t chain, double *out) {
   const int P = ctx->ds[c.dataset].P;
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
-  CK(cudaMemcpy(out, c.dev.omega_d, sizeof(double) * P * P, cudaMemcpyDeviceToHost));
+  CK(d2h(ctx, out, c.dev.omega_d, sizeof(double) * P * P));
   return BSG_OK;
 }
 
@@ -1022,8 +1043,8 @@ bsg_status bsg_set_omega(bsg_ctx *ctx, int32_t chain, const double *in) {
   std::vector<float> f(in, in + P * P);
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
-  CK(cudaMemcpy(c.dev.omega_d, in, sizeof(double) * P * P, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(c.dev.omega_f, f.data(), sizeof(float) * P * P, cudaMemcpyHostToDevice));
+  CK(h2d(ctx, c.dev.omega_d, in, sizeof(double) * P * P));
+  CK(h2d(ctx, c.dev.omega_f, f.data(), sizeof(float) * P * P));
   return BSG_OK;
 }
 
@@ -1032,8 +1053,7 @@ bsg_status bsg_set_beta_wm(bsg_ctx *ctx, int32_t chain, float beta_wm) {
   Chain &c = ctx->ch[chain];
   c.desc.beta_wm = beta_wm;
   CK(cudaSetDevice(ctx->device));
-  CK(cudaMemcpyAsync(c.dev.wm_beta, &beta_wm, sizeof(float), cudaMemcpyHostToDevice,
-                     ctx->stream));
+  CK(h2d(ctx, c.dev.wm_beta, &beta_wm, sizeof(float)));
   CK(cudaStreamSynchronize(ctx->stream));
   return BSG_OK;
 }
@@ -1065,9 +1085,9 @@ bsg_status bsg_get_beta_wm(bsg_ctx *ctx, int32_t chain, float *beta_wm,
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   WmState w{};
-  CK(cudaMemcpy(&w, c.dev.wm_sum, sizeof(w), cudaMemcpyDeviceToHost));
+  CK(d2h(ctx, &w, c.dev.wm_sum, sizeof(w)));
   long long nk = 0;
-  CK(cudaMemcpy(&nk, c.dev.nkept, sizeof(nk), cudaMemcpyDeviceToHost));
+  CK(d2h(ctx, &nk, c.dev.nkept, sizeof(nk)));
   if (beta_wm) *beta_wm = w.beta;
   if (mean_kept) *mean_kept = nk > 0 ? w.sum / (double)nk : 0.0;
   return BSG_OK;
@@ -1078,8 +1098,7 @@ bsg_status bsg_get_colmeans(bsg_ctx *ctx, int32_t chain, float *out) {
   const Chain &c = ctx->ch[chain];
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
-  CK(cudaMemcpy(out, c.dev.colmean, sizeof(float) * ctx->ds[c.dataset].P,
-                cudaMemcpyDeviceToHost));
+  CK(d2h(ctx, out, c.dev.colmean, sizeof(float) * ctx->ds[c.dataset].P));
   return BSG_OK;
 }
 
@@ -1088,7 +1107,7 @@ bsg_status bsg_get_sweep(bsg_ctx *ctx, int32_t chain, int64_t *sweep, int64_t *n
   ChainCounters h{};
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
-  CK(cudaMemcpy(&h, counters_of(ctx->ch[chain]), sizeof(h), cudaMemcpyDeviceToHost));
+  CK(d2h(ctx, &h, counters_of(ctx->ch[chain]), sizeof(h)));
   if (sweep) *sweep = h.sweep[1];
   if (nkept) *nkept = h.nkept;
   return BSG_OK;
@@ -1107,7 +1126,7 @@ bsg_status bsg_compute_prb(bsg_ctx *ctx, int32_t chain, float *prb) {
   float *dp = (float *)dalloc(ctx, sizeof(float) * n, &e);
   CK(e);
   CK(launch_prb(ctx->d_ds, ctx->d_ch, chain, d.dev, dp, ctx->stream));
-  CK(cudaMemcpyAsync(prb, dp, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(d2h(ctx, prb, dp, sizeof(float) * n));
   CK(cudaStreamSynchronize(ctx->stream));
   dfree(ctx, dp);
   return BSG_OK;
@@ -1124,8 +1143,8 @@ bsg_status bsg_get_posterior(bsg_ctx *ctx, int32_t chain, double *mean,
   const size_t n = (size_t)d.P * d.V;
   // mean = sum / T, var = (sum2 - T mean^2) / (T - 1)  (mcmc.cpp:877-881)
   std::vector<double> sum(n), sq(n);
-  CK(cudaMemcpy(sum.data(), c.dev.acc_sum, sizeof(double) * n, cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(sq.data(), c.dev.acc_sq, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  CK(d2h(ctx, sum.data(), c.dev.acc_sum, sizeof(double) * n));
+  CK(d2h(ctx, sq.data(), c.dev.acc_sq, sizeof(double) * n));
   const double T = (double)nk;
   for (size_t i = 0; i < n; ++i) {
     const double m = sum[i] / T;
@@ -1133,8 +1152,7 @@ bsg_status bsg_get_posterior(bsg_ctx *ctx, int32_t chain, double *mean,
     if (var) var[i] = (sq[i] - T * m * m) / (T - 1.0);
   }
   if (prb && d.S) {
-    CK(cudaMemcpy(prb, c.dev.prb_sum, sizeof(double) * (size_t)d.S * d.V,
-                  cudaMemcpyDeviceToHost));
+    CK(d2h(ctx, prb, c.dev.prb_sum, sizeof(double) * (size_t)d.S * d.V));
     for (size_t i = 0; i < (size_t)d.S * d.V; ++i) prb[i] /= T;
   }
   if (nkept) *nkept = nk;
@@ -1183,15 +1201,15 @@ bsg_status bsg_reset_accumulators(bsg_ctx *ctx, int32_t chain) {
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   const size_t n = (size_t)d.P * d.V;
-  CK(cudaMemset(c.dev.acc_sum, 0, sizeof(double) * n));
-  CK(cudaMemset(c.dev.acc_sq, 0, sizeof(double) * n));
-  if (d.S) CK(cudaMemset(c.dev.prb_sum, 0, sizeof(double) * (size_t)d.S * d.V));
-  CK(cudaMemset(c.dev.nkept, 0, sizeof(long long)));
-  CK(cudaMemset(c.dev.wm_sum, 0, sizeof(double)));
+  CK(cudaMemsetAsync(c.dev.acc_sum, 0, sizeof(double) * n, ctx->stream));
+  CK(cudaMemsetAsync(c.dev.acc_sq, 0, sizeof(double) * n, ctx->stream));
+  if (d.S) CK(cudaMemsetAsync(c.dev.prb_sum, 0, sizeof(double) * (size_t)d.S * d.V, ctx->stream));
+  CK(cudaMemsetAsync(c.dev.nkept, 0, sizeof(long long), ctx->stream));
+  CK(cudaMemsetAsync(c.dev.wm_sum, 0, sizeof(double), ctx->stream));
   if (c.dev.pred_part) {
-    CK(cudaMemset(c.dev.qhat, 0, sizeof(double) * (size_t)d.N * std::max(d.S, 1)));
-    CK(cudaMemset(c.dev.pred_sums, 0, sizeof(double) * 2));
-    CK(cudaMemset(c.dev.npred, 0, sizeof(long long)));
+    CK(cudaMemsetAsync(c.dev.qhat, 0, sizeof(double) * (size_t)d.N * std::max(d.S, 1), ctx->stream));
+    CK(cudaMemsetAsync(c.dev.pred_sums, 0, sizeof(double) * 2, ctx->stream));
+    CK(cudaMemsetAsync(c.dev.npred, 0, sizeof(long long), ctx->stream));
   }
   return BSG_OK;
 }
@@ -1256,13 +1274,13 @@ bsg_status bsg_checkpoint(bsg_ctx *ctx, int32_t chain, void *buf, int64_t size) 
   CK(cudaStreamSynchronize(ctx->stream));
   char *p = static_cast<char *>(buf);
   WmState ws{};
-  CK(cudaMemcpy(&ws, c.dev.wm_sum, sizeof(ws), cudaMemcpyDeviceToHost));
+  CK(d2h(ctx, &ws, c.dev.wm_sum, sizeof(ws)));
   CkptHeader h{kCkptMagic, 2, d.P, d.Vp, d.V, d.S, c.dev.df_offset, c.dev.burnin,
                c.dev.thin, c.dev.key0, c.dev.key1, c.dev.chain_id, ws.beta};
   std::memcpy(p, &h, sizeof(h));
   p += sizeof(h);
   auto get = [&](const void *src, size_t n) -> cudaError_t {
-    cudaError_t e = cudaMemcpy(p, src, n, cudaMemcpyDeviceToHost);
+    cudaError_t e = d2h(ctx, p, src, n);
     p += n;
     return e;
   };
@@ -1275,8 +1293,8 @@ bsg_status bsg_checkpoint(bsg_ctx *ctx, int32_t chain, void *buf, int64_t size) 
   const size_t nq = (size_t)d.N * std::max(d.S, 1);
   PredCkpt pk{c.pred_on ? 1 : 0, c.dev.pred_part ? 1 : 0, 0, 0.0};
   if (c.dev.pred_part) {
-    CK(cudaMemcpy(&pk.npred, c.dev.npred, sizeof(long long), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(&pk.ed_sum, c.dev.pred_sums, sizeof(double), cudaMemcpyDeviceToHost));
+    CK(d2h(ctx, &pk.npred, c.dev.npred, sizeof(long long)));
+    CK(d2h(ctx, &pk.ed_sum, c.dev.pred_sums, sizeof(double)));
   }
   std::memcpy(p, &pk, sizeof(pk));
   p += sizeof(pk);
@@ -1321,7 +1339,7 @@ bsg_status bsg_restore(bsg_ctx *ctx, int32_t chain, const void *buf, int64_t siz
   CK(cudaStreamSynchronize(ctx->stream));
   const char *p = static_cast<const char *>(buf) + sizeof(h);
   auto put = [&](void *dst, size_t n) -> cudaError_t {
-    cudaError_t e = cudaMemcpy(dst, p, n, cudaMemcpyHostToDevice);
+    cudaError_t e = h2d(ctx, dst, p, n);
     p += n;
     return e;
   };
@@ -1330,8 +1348,7 @@ bsg_status bsg_restore(bsg_ctx *ctx, int32_t chain, const void *buf, int64_t siz
   std::memcpy(om.data(), p, sizeof(double) * om.size());
   CK(put(c.dev.omega_d, sizeof(double) * om.size()));
   std::vector<float> omf(om.begin(), om.end());
-  CK(cudaMemcpy(c.dev.omega_f, omf.data(), sizeof(float) * omf.size(),
-                cudaMemcpyHostToDevice));
+  CK(h2d(ctx, c.dev.omega_f, omf.data(), sizeof(float) * omf.size()));
   CK(put(counters_of(c), sizeof(ChainCounters)));
   CK(put(c.dev.acc_sum, sizeof(double) * (size_t)d.P * d.V));
   CK(put(c.dev.acc_sq, sizeof(double) * (size_t)d.P * d.V));
@@ -1346,12 +1363,12 @@ bsg_status bsg_restore(bsg_ctx *ctx, int32_t chain, const void *buf, int64_t siz
     bsg_status ps = ensure_pred(ctx, c);
     if (ps) return ps;
     if (pk.allocated)
-      CK(cudaMemcpy(c.dev.qhat, p, sizeof(double) * nq, cudaMemcpyHostToDevice));
+      CK(h2d(ctx, c.dev.qhat, p, sizeof(double) * nq));
     else
-      CK(cudaMemset(c.dev.qhat, 0, sizeof(double) * nq));
-    CK(cudaMemcpy(c.dev.npred, &pk.npred, sizeof(long long), cudaMemcpyHostToDevice));
+      CK(cudaMemsetAsync(c.dev.qhat, 0, sizeof(double) * nq, ctx->stream));
+    CK(h2d(ctx, c.dev.npred, &pk.npred, sizeof(long long)));
     const double sums[2] = {pk.ed_sum, 0.0};
-    CK(cudaMemcpy(c.dev.pred_sums, sums, sizeof(sums), cudaMemcpyHostToDevice));
+    CK(h2d(ctx, c.dev.pred_sums, sums, sizeof(sums)));
   }
   if (h.version == 2) p += sizeof(double) * nq;
   c.pred_on = pk.on != 0;
@@ -1361,13 +1378,13 @@ bsg_status bsg_restore(bsg_ctx *ctx, int32_t chain, const void *buf, int64_t siz
     p += sizeof(wk) + sizeof(MixCkpt);
   } else {
     long long nk = 0;  // v1: beta_WM was fixed, so its kept sum is nk beta_WM
-    CK(cudaMemcpy(&nk, c.dev.nkept, sizeof(nk), cudaMemcpyDeviceToHost));
+    CK(d2h(ctx, &nk, c.dev.nkept, sizeof(nk)));
     wk.sum = (double)nk * (double)h.beta_wm;
   }
   if (wk.update && !d.dev.has_c)
     return fail(ctx, BSG_ERR_UNSUPPORTED, "checkpoint has the beta_WM update on");
   const WmState ws{wk.sum, h.beta_wm, 0};
-  CK(cudaMemcpy(c.dev.wm_sum, &ws, sizeof(ws), cudaMemcpyHostToDevice));
+  CK(h2d(ctx, c.dev.wm_sum, &ws, sizeof(ws)));
   c.dev.wm_update = wk.update;
   if (mk.model != c.dev.model) {
     bsg_status ms = set_model(ctx, c, mk.model);
@@ -1520,8 +1537,7 @@ bsg_status bsg_predict(bsg_ctx *ctx, int32_t chain, double *mpredict) {
                            (d.N + kPredWarps - 1) / kPredWarps, chain, kPredNow,
                            ctx->stream, false));
   CK(cudaStreamSynchronize(ctx->stream));
-  CK(cudaMemcpy(mpredict, c.dev.mpred, sizeof(double) * (size_t)d.N * d.S,
-                cudaMemcpyDeviceToHost));
+  CK(d2h(ctx, mpredict, c.dev.mpred, sizeof(double) * (size_t)d.N * d.S));
   return BSG_OK;
 }
 
@@ -1536,9 +1552,9 @@ bsg_status bsg_get_predictive(bsg_ctx *ctx, int32_t chain, double *qhat,
   long long n = 0;
   double ed = 0.0;
   if (c.dev.pred_part) {
-    CK(cudaMemcpy(&n, c.dev.npred, sizeof(n), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(&ed, c.dev.pred_sums, sizeof(ed), cudaMemcpyDeviceToHost));
-    if (qhat && nq) CK(cudaMemcpy(qhat, c.dev.qhat, sizeof(double) * nq, cudaMemcpyDeviceToHost));
+    CK(d2h(ctx, &n, c.dev.npred, sizeof(n)));
+    CK(d2h(ctx, &ed, c.dev.pred_sums, sizeof(ed)));
+    if (qhat && nq) CK(d2h(ctx, qhat, c.dev.qhat, sizeof(double) * nq));
   } else if (qhat && nq) {
     std::memset(qhat, 0, sizeof(double) * nq);
   }
@@ -1554,8 +1570,8 @@ bsg_status bsg_get_dic(bsg_ctx *ctx, int32_t chain, double *dic) {
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   long long nk = 0, np = 0;
-  CK(cudaMemcpy(&nk, c.dev.nkept, sizeof(nk), cudaMemcpyDeviceToHost));
-  if (c.dev.pred_part) CK(cudaMemcpy(&np, c.dev.npred, sizeof(np), cudaMemcpyDeviceToHost));
+  CK(d2h(ctx, &nk, c.dev.nkept, sizeof(nk)));
+  if (c.dev.pred_part) CK(d2h(ctx, &np, c.dev.npred, sizeof(np)));
   if (nk < 1 || np < 1)
     return fail(ctx, BSG_ERR_STATE,
                 "DIC needs kept sweeps with the predictive pass on (bsg_set_predictive)");
@@ -1569,7 +1585,7 @@ bsg_status bsg_get_dic(bsg_ctx *ctx, int32_t chain, double *dic) {
                            ctx->stream, false));
   CK(cudaStreamSynchronize(ctx->stream));
   double sums[2];
-  CK(cudaMemcpy(sums, c.dev.pred_sums, sizeof(sums), cudaMemcpyDeviceToHost));
+  CK(d2h(ctx, sums, c.dev.pred_sums, sizeof(sums)));
   // mcmc.cpp:966-975
   const double DE = sums[1];
   const double ED = -2.0 * sums[0] / (double)np;

@@ -106,3 +106,34 @@ def test_mcmc_convenience_equals_sampler():
     assert np.array_equal(out["spatCoef"], maps["spatCoef"])
     assert out["DIC"] == dic and out["beta_WM"] == cur
     assert np.array_equal(out["bWM"][mask.astype(bool)], mean * wm.astype(np.float64))
+
+
+def test_reset_accumulators_is_ordered_with_the_sweeps():
+    """bsg_reset_accumulators clears the running sums on the context stream:
+    with four chains of a mid-sized study, the posterior after a reset and
+    six single sweeps is exactly the mean and sample variance of the six
+    recorded coefficient maps (a clear that raced the following sweeps would
+    leave stale sums and negative variances)."""
+    import bsglmm_gb300 as bsg
+    mask, covar, data, S = _study(31, (48, 44, 40), 128, 3)
+    with bsg.Sampler() as s:
+        ds = s.add_dataset(mask, covar, data, S)
+        chs = [s.add_chain(ds, seed=100 + k, burnin=0, thin=1) for k in range(4)]
+        lat = s.lattice(ds)
+        inmask = lat["idx"] >= 0
+        cols = lat["idxsc"][inmask][np.argsort(lat["idx"][inmask])]
+        s.run(5)
+        for ch in chs:
+            s.reset_accumulators(ch)
+        trace = {ch: [] for ch in chs}
+        for _ in range(6):
+            s.run(1)
+            for ch in chs:
+                trace[ch].append(s.beta(ch)[:, cols].astype(np.float64))
+        for ch in chs:
+            mean, var, _, nk = s.posterior(ch)
+            tr = np.stack(trace[ch])
+            assert nk == 6
+            assert np.allclose(mean, tr.mean(0), rtol=1e-12, atol=1e-12)
+            assert np.allclose(var, tr.var(0, ddof=1), rtol=1e-6, atol=1e-9)
+            assert var.min() > -1e-9

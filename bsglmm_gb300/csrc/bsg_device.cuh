@@ -102,14 +102,33 @@ template <bool CLAMP = false>
 __device__ __forceinline__ float tn_lower_inv(float a, uint32_t k) {
   const float T = phi_tail(fabsf(a));
   const float uc = u_of(~k);
-  const float tuc = T * uc;
+  const float tuc = __fmul_rn(T, uc);
   const float q1 = fmaf(T, uc, u_of(k));
   const bool neg = a < 0.f;
   const bool lo = neg && q1 < 0.5f;
-  float arg = lo ? q1 : (neg ? uc - tuc : tuc);
+  float arg = lo ? q1 : (neg ? __fsub_rn(uc, tuc) : tuc);
   if (CLAMP) arg = fmaxf(arg, 1.17549435e-38f);
   const float t = ndtri_lower(arg);
   return lo ? t : -t;
+}
+
+// Two draws of tn_lower_inv (CLAMP off) with the paired f32x2 arithmetic:
+// exactly (tn_lower_inv(a.x, k0), tn_lower_inv(a.y, k1)) in half the FP32
+// instructions.
+__device__ __forceinline__ float2 u_of2(uint32_t k0, uint32_t k1) {
+  return fma2(make_float2((float)k0, (float)k1), splat2(0x1p-32f), splat2(0x1p-33f));
+}
+__device__ __forceinline__ float2 tn_lower_inv2(float2 a, uint32_t k0, uint32_t k1) {
+  const float2 T = phi_tail2(make_float2(fabsf(a.x), fabsf(a.y)));
+  const float2 uc = u_of2(~k0, ~k1);
+  const float2 tuc = mul2(T, uc);
+  const float2 q1 = fma2(T, uc, u_of2(k0, k1));
+  const float2 dd = sub2(uc, tuc);
+  const bool n0 = a.x < 0.f, n1 = a.y < 0.f;
+  const bool lo0 = n0 && q1.x < 0.5f, lo1 = n1 && q1.y < 0.5f;
+  const float2 t = ndtri_lower2(make_float2(lo0 ? q1.x : (n0 ? dd.x : tuc.x),
+                                            lo1 ? q1.y : (n1 ? dd.y : tuc.y)));
+  return make_float2(lo0 ? t.x : -t.x, lo1 ? t.y : -t.y);
 }
 
 // Far tail a > kATail: Robert (1995) exponential proposal with rate

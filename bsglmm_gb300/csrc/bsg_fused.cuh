@@ -51,7 +51,15 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
                         Supplied sup) {
   constexpr int NT = P * (P + 1) / 2;
   constexpr int PP = P <= 4 ? 4 : 8;  // design row padded to float4s
-  __shared__ __align__(16) float Xs[kChunkPad][PP];
+  // The probit kernel stages the design as subject pairs: pair row m holds
+  // (x_2m,p, x_2m+1,p) for p = 0..P-1, so one f32x2 operation serves two
+  // subjects; a pad of 4 floats after every 16 pair rows keeps the lanes of
+  // a voxel (32 subjects = 16 pair rows apart) on distinct banks.  The
+  // other kernels keep one padded row per subject (a pad row per 32).
+  constexpr bool PAIRX = !MIX && !SUPP;
+  constexpr int RW = 2 * ((P + 1) & ~1);  // floats per pair row
+  constexpr int XS_FLOATS = PAIRX ? (kChunk / 2) * RW + (kChunk / 32) * 4 : kChunkPad * PP;
+  __shared__ __align__(16) float Xs[XS_FLOATS];
   __shared__ float Om[P * P], Xtx[P * P];
 
   const BlockMap bm = map[blockIdx.x];
@@ -89,6 +97,14 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
   }
 #pragma unroll
   for (int p = 0; p < P; ++p) acc[p] = 0.f;
+  // PAIRX: the coefficients duplicated into both halves of an f32x2 operand,
+  // and X'(Z - b_WM WM) of the even (.x) and odd (.y) subjects
+  float2 bb[PAIRX ? P : 1], acc2[PAIRX ? P : 1];
+#pragma unroll
+  for (int p = 0; p < (PAIRX ? P : 1); ++p) {
+    bb[p] = make_float2(beta[p], beta[p]);
+    acc2[p] = make_float2(0.f, 0.f);
+  }
   constexpr int NQ = MIX ? NT : 1;
   float qw[NQ];  // MIX: this voxel's X' Phi X, packed lower
 #pragma unroll
@@ -104,7 +120,13 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
     __syncthreads();
     for (int t = tid; t < P * kChunk; t += blockDim.x) {
       const int p = t / kChunk, ii = t - p * kChunk;
-      Xs[ii + (ii >> 5)][p] = ii < cn ? d.covar[(size_t)p * N + i0 + ii] : 0.f;
+      const float xv = ii < cn ? d.covar[(size_t)p * N + i0 + ii] : 0.f;
+      if constexpr (PAIRX) {
+        const int m = ii >> 1;
+        Xs[m * RW + (m >> 4) * 4 + 2 * p + (ii & 1)] = xv;
+      } else {
+        Xs[(ii + (ii >> 5)) * PP + p] = xv;
+      }
     }
     __syncthreads();
     if (active) {
@@ -114,17 +136,24 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
       auto subject = [&](int col, uint32_t ymask, uint32_t kk, uint32_t isub,
                          uint32_t gn, uint32_t gu, float ph) {
         float x[P];
-        const float4 v0 = *reinterpret_cast<const float4 *>(&Xs[col][0]);
-        x[0] = v0.x;
-        if (P > 1) x[1] = v0.y;
-        if (P > 2) x[2] = v0.z;
-        if (P > 3) x[3] = v0.w;
-        if (P > 4) {
-          const float4 v1 = *reinterpret_cast<const float4 *>(&Xs[col][4]);
-          x[4] = v1.x;
-          if (P > 5) x[5] = v1.y;
-          if (P > 6) x[6] = v1.z;
-          if (P > 7) x[7] = v1.w;
+        if constexpr (PAIRX) {
+          const int ii = col - col / 33, m = ii >> 1;  // col = ii + ii / 32
+          const float *xr = &Xs[m * RW + (m >> 4) * 4 + (ii & 1)];
+#pragma unroll
+          for (int p = 0; p < P; ++p) x[p] = xr[2 * p];
+        } else {
+          const float4 v0 = *reinterpret_cast<const float4 *>(&Xs[col * PP]);
+          x[0] = v0.x;
+          if (P > 1) x[1] = v0.y;
+          if (P > 2) x[2] = v0.z;
+          if (P > 3) x[3] = v0.w;
+          if (P > 4) {
+            const float4 v1 = *reinterpret_cast<const float4 *>(&Xs[col * PP + 4]);
+            x[4] = v1.x;
+            if (P > 5) x[5] = v1.y;
+            if (P > 6) x[6] = v1.z;
+            if (P > 7) x[7] = v1.w;
+          }
         }
         float m0 = 0.f;
 #pragma unroll
@@ -179,42 +208,49 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
         }
         const float zr = m0 + __uint_as_float(__float_as_uint(t) ^ ymask ^ 0x80000000u);
 #pragma unroll
-        for (int p = 0; p < P; ++p) acc[p] = fmaf(x[p], zr, acc[p]);
+        for (int p = 0; p < P; ++p) {
+          if constexpr (PAIRX)
+            acc2[p].x = fmaf(x[p], zr, acc2[p].x);
+          else
+            acc[p] = fmaf(x[p], zr, acc[p]);
+        }
       };
-      // Probit with Philox variates, four subjects of one Philox call: the
-      // four inversion draws carry no control flow (so their dependency
-      // chains interleave), one vote per group sends the rare subjects
-      // beyond kATail to the bounded rejection sampler, then X'(Z - bwm)
-      // takes the four in order.  The same arithmetic as `subject`.
-      auto group4 = [&](int col0, uint32_t yw4, uint4 r, uint32_t i) {
-        float m0q[4], aq[4], zq[4];
-        auto row = [&](int col, float (&x)[P]) {
-          const float4 v0 = *reinterpret_cast<const float4 *>(&Xs[col][0]);
-          x[0] = v0.x;
-          if (P > 1) x[1] = v0.y;
-          if (P > 2) x[2] = v0.z;
-          if (P > 3) x[3] = v0.w;
-          if (P > 4) {
-            const float4 v1 = *reinterpret_cast<const float4 *>(&Xs[col][4]);
-            x[4] = v1.x;
-            if (P > 5) x[5] = v1.y;
-            if (P > 6) x[6] = v1.z;
-            if (P > 7) x[7] = v1.w;
+      // The probit group of four on subject pairs (PAIRX): x'beta, the
+      // inversion and X'(Z - bwm) each as two f32x2 pairs, subjects
+      // (ii0, ii0 + 1) and (ii0 + 2, ii0 + 3).  Per subject the same
+      // arithmetic as `subject`; the even and odd subjects' X'Z sums are
+      // kept apart until the end of the voxel.
+      auto group4p = [&](int ii0, uint32_t yw4, uint4 r, uint32_t i) {
+        const int m = ii0 >> 1;  // even: rows m, m + 1 share one pad group
+        const float *xr0 = &Xs[m * RW + (m >> 4) * 4];
+        float2 m0h[2], zh[2];
+        float aq[4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const float *xr = xr0 + h * RW;
+          float2 s = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int p = 0; p + 1 < P; p += 2) {
+            const float4 v4 = *reinterpret_cast<const float4 *>(xr + 2 * p);
+            s = fma2(make_float2(v4.x, v4.y), bb[p], s);
+            s = fma2(make_float2(v4.z, v4.w), bb[p + 1], s);
           }
-        };
+          if (P & 1)
+            s = fma2(*reinterpret_cast<const float2 *>(xr + 2 * (P - 1)), bb[P - 1], s);
+          m0h[h] = s;
+          const float2 a = add2(s, make_float2(bwm, bwm));
+          aq[2 * h] = __uint_as_float(__float_as_uint(a.x) ^ ((yw4 >> (2 * h)) << 31));
+          aq[2 * h + 1] = __uint_as_float(__float_as_uint(a.y) ^ ((yw4 >> (2 * h + 1)) << 31));
+        }
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          float x[P];
-          row(col0 + q, x);
-          float m0 = 0.f;
-#pragma unroll
-          for (int p = 0; p < P; ++p) m0 = fmaf(beta[p], x[p], m0);
-          const uint32_t ym = (yw4 >> q) << 31;
-          const float a = __uint_as_float(__float_as_uint(m0 + bwm) ^ ym);
-          const float t = tn_lower_inv(fminf(a, kATail), pick4(r, q));
-          m0q[q] = m0;
-          aq[q] = a;
-          zq[q] = m0 + __uint_as_float(__float_as_uint(t) ^ ym ^ 0x80000000u);
+        for (int h = 0; h < 2; ++h) {
+          const float2 t = tn_lower_inv2(
+              make_float2(fminf(aq[2 * h], kATail), fminf(aq[2 * h + 1], kATail)),
+              pick4(r, 2 * h), pick4(r, 2 * h + 1));
+          const uint32_t y0 = (yw4 >> (2 * h)) << 31, y1 = (yw4 >> (2 * h + 1)) << 31;
+          zh[h] = add2(m0h[h],
+                       make_float2(__uint_as_float(__float_as_uint(t.x) ^ y0 ^ 0x80000000u),
+                                   __uint_as_float(__float_as_uint(t.y) ^ y1 ^ 0x80000000u)));
         }
         const bool far = fmaxf(fmaxf(aq[0], aq[1]), fmaxf(aq[2], aq[3])) > kATail;
         if (__any_sync(__activemask(), far)) {
@@ -224,15 +260,26 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
               const uint32_t ym = (yw4 >> q) << 31;
               const float t = tn_lower_tail(aq[q], i + q, (uint32_t)v, sweep,
                                             cid | kTagZTail, ch.key0, ch.key1, &ok);
-              zq[q] = m0q[q] + __uint_as_float(__float_as_uint(t) ^ ym ^ 0x80000000u);
+              const float m0 = (q & 1) ? m0h[q >> 1].y : m0h[q >> 1].x;
+              const float z = m0 + __uint_as_float(__float_as_uint(t) ^ ym ^ 0x80000000u);
+              if (q & 1)
+                zh[q >> 1].y = z;
+              else
+                zh[q >> 1].x = z;
             }
         }
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          float x[P];
-          row(col0 + q, x);
+        for (int h = 0; h < 2; ++h) {
+          const float *xr = xr0 + h * RW;
 #pragma unroll
-          for (int p = 0; p < P; ++p) acc[p] = fmaf(x[p], zq[q], acc[p]);
+          for (int p = 0; p + 1 < P; p += 2) {
+            const float4 v4 = *reinterpret_cast<const float4 *>(xr + 2 * p);
+            acc2[p] = fma2(make_float2(v4.x, v4.y), zh[h], acc2[p]);
+            acc2[p + 1] = fma2(make_float2(v4.z, v4.w), zh[h], acc2[p + 1]);
+          }
+          if (P & 1)
+            acc2[P - 1] = fma2(*reinterpret_cast<const float2 *>(xr + 2 * (P - 1)), zh[h],
+                               acc2[P - 1]);
         }
       };
       // The t/logit links, four subjects: Z by inversion and the first
@@ -244,13 +291,13 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
         float m0q[4], aq[4], sdq[4], rq[4], gq[4];
         bool bad[4];
         auto row = [&](int col, float (&x)[P]) {
-          const float4 v0 = *reinterpret_cast<const float4 *>(&Xs[col][0]);
+          const float4 v0 = *reinterpret_cast<const float4 *>(&Xs[col * PP]);
           x[0] = v0.x;
           if (P > 1) x[1] = v0.y;
           if (P > 2) x[2] = v0.z;
           if (P > 3) x[3] = v0.w;
           if (P > 4) {
-            const float4 v1 = *reinterpret_cast<const float4 *>(&Xs[col][4]);
+            const float4 v1 = *reinterpret_cast<const float4 *>(&Xs[col * PP + 4]);
             x[4] = v1.x;
             if (P > 5) x[5] = v1.y;
             if (P > 6) x[6] = v1.z;
@@ -358,8 +405,8 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
             }
             uint4 r = make_uint4(0, 0, 0, 0);
             if (!SUPP) r = philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key);
-            if constexpr (!MIX && !SUPP) {
-              group4(xo + b, yw, r, i);
+            if constexpr (PAIRX) {
+              group4p((wl << 5) + b, yw, r, i);
               yw >>= 4;
             } else if constexpr (MIX) {
               group4_mix(xo + b, yw, r, i, gpair(i), gpair(i + 2), phc);
@@ -384,9 +431,9 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
             const uint32_t i = i00 + (uint32_t)b;
             uint4 r = make_uint4(0, 0, 0, 0);
             if (!SUPP) r = philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key);
-            if constexpr (!MIX && !SUPP) {
+            if constexpr (PAIRX) {
               if (b + 4 <= nbits) {  // a whole group of the last word
-                group4(xo + b, yw, r, i);
+                group4p((wl << 5) + b, yw, r, i);
                 yw >>= 4;
                 continue;
               }
@@ -407,6 +454,10 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
     }
   }
 
+  if constexpr (PAIRX) {
+#pragma unroll
+    for (int p = 0; p < P; ++p) acc[p] = acc2[p].x + acc2[p].y;
+  }
   if (LPV > 1) {
 #pragma unroll
     for (int p = 0; p < P; ++p)

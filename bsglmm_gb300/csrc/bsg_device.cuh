@@ -159,17 +159,48 @@ static __device__ __noinline__ float tn_lower_tail(float a, uint32_t i, uint32_t
 // d = alpha - 1/3 and c = 1/sqrt(9 d) from a normal (bits kn) and a uniform
 // (bits ku): g = d v^3 with v = 1 + c x, accepted by the squeeze
 // u < 1 - 0.0331 x^4 or by log u < x^2/2 + d (1 - v^3 + log v^3).
+// Products and sums are stated with explicit rounding (no contraction), so
+// gamma_mt_try2 below decides exactly as two calls of this function.
 __device__ __forceinline__ bool gamma_mt_try(float d, float c, uint32_t kn,
                                              uint32_t ku, float *g) {
   const float x = normal_of(kn);
   const float v = fmaf(c, x, 1.f);
-  const float v3 = v * v * v;
-  *g = d * v3;
+  const float v3 = __fmul_rn(__fmul_rn(v, v), v);
+  *g = __fmul_rn(d, v3);
   if (!(v > 0.f)) return false;
-  const float u = u_of(ku), x2 = x * x;
-  if (u < fmaf(-0.0331f * x2, x2, 1.f)) return true;
-  return lg2_approx(u) * 0.693147181f <
-         fmaf(0.5f, x2, d * (1.f - v3 + lg2_approx(v3) * 0.693147181f));
+  const float u = u_of(ku), x2 = __fmul_rn(x, x);
+  if (u < fmaf(__fmul_rn(-0.0331f, x2), x2, 1.f)) return true;
+  return __fmul_rn(lg2_approx(u), kLn2) <
+         fmaf(0.5f, x2, __fmul_rn(d, fmaf(lg2_approx(v3), kLn2, __fsub_rn(1.f, v3))));
+}
+
+// Standard normals of two words by inversion: exactly (normal_of(k0),
+// normal_of(k1)).
+__device__ __forceinline__ float2 normal_of2(uint32_t k0, uint32_t k1) {
+  const bool l0 = k0 < 0x80000000u, l1 = k1 < 0x80000000u;
+  const float2 t = ndtri_lower2(u_of2(l0 ? k0 : ~k0, l1 ? k1 : ~k1));
+  return make_float2(l0 ? t.x : -t.x, l1 ? t.y : -t.y);
+}
+
+// Two first attempts of gamma_mt_try in f32x2 pairs, without control flow:
+// g = (d v0^3, d v1^3) and the two acceptance decisions, exactly as two
+// scalar calls.
+__device__ __forceinline__ void gamma_mt_try2(float d, float c, uint32_t kn0, uint32_t kn1,
+                                              uint32_t ku0, uint32_t ku1, float2 *g,
+                                              bool *ok0, bool *ok1) {
+  const float2 x = normal_of2(kn0, kn1);
+  const float2 v = fma2(splat2(c), x, splat2(1.f));
+  const float2 v3 = mul2(mul2(v, v), v);
+  *g = mul2(splat2(d), v3);
+  const float2 u = u_of2(ku0, ku1), x2 = mul2(x, x);
+  const float2 sq = fma2(mul2(splat2(-0.0331f), x2), x2, splat2(1.f));
+  const float2 lu = mul2(make_float2(lg2_approx(u.x), lg2_approx(u.y)), splat2(kLn2));
+  const float2 rhs =
+      fma2(splat2(0.5f), x2,
+           mul2(splat2(d), fma2(make_float2(lg2_approx(v3.x), lg2_approx(v3.y)),
+                                splat2(kLn2), sub2(splat2(1.f), v3))));
+  *ok0 = v.x > 0.f && (u.x < sq.x || lu.x < rhs.x);
+  *ok1 = v.y > 0.f && (u.y < sq.y || lu.y < rhs.y);
 }
 
 // Further attempts after a rejected first one: attempt pairs from counters

@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
           float gm;
           if (ch.t_df == 3.f) {
             // Gamma(2, 1) = Exp(1) + Exp(1) = -ln(u1 u2), exactly (t link)
-            gm = lg2_approx(u_of(gn) * u_of(gu)) * -0.693147181f;
+            gm = __fmul_rn(lg2_approx(__fmul_rn(u_of(gn), u_of(gu))), -kLn2);
           } else if (!gamma_mt_try(ch.mix_d, ch.mix_c, gn, gu, &gm)) {
             gm = gamma_mt_more(ch.mix_d, ch.mix_c, isub, (uint32_t)v, sweep,
                                cid | kTagPhiMore, ch.key0, ch.key1, &ok);
@@ -315,22 +315,39 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
           const uint32_t ym = (yw4 >> q) << 31;
           const float ph = ph4[q];
           const float sd = rsqrt_approx(ph);
-          const float a = __uint_as_float(__float_as_uint((m0 + bwm) * (ph * sd)) ^ ym);
-          const float t = tn_lower_inv(fminf(a, kATail), pick4(r, q));
           m0q[q] = m0;
-          aq[q] = a;
           sdq[q] = sd;
-          rq[q] = __uint_as_float(__float_as_uint(t * sd) ^ ym ^ 0x80000000u);
-          const uint4 gg = q < 2 ? g0 : g1;
-          const uint32_t gn = (q & 1) ? gg.z : gg.x, gu = (q & 1) ? gg.w : gg.y;
-          float g;
+          aq[q] = __uint_as_float(__float_as_uint((m0 + bwm) * (ph * sd)) ^ ym);
+        }
+        // the inversions and the first gamma attempts as f32x2 pairs:
+        // subjects (0, 1) and (2, 3); the gamma words of subject 2h + s are
+        // (gn, gu) = (.x, .y) for s = 0 and (.z, .w) for s = 1 of g_h
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int q0 = 2 * h, q1 = q0 + 1;
+          const float2 t = tn_lower_inv2(
+              make_float2(fminf(aq[q0], kATail), fminf(aq[q1], kATail)), pick4(r, q0),
+              pick4(r, q1));
+          const float2 rr = mul2(t, make_float2(sdq[q0], sdq[q1]));
+          rq[q0] = __uint_as_float(__float_as_uint(rr.x) ^ ((yw4 >> q0) << 31) ^ 0x80000000u);
+          rq[q1] = __uint_as_float(__float_as_uint(rr.y) ^ ((yw4 >> q1) << 31) ^ 0x80000000u);
+          const uint4 gg = h ? g1 : g0;
           if (t3) {
-            g = lg2_approx(u_of(gn) * u_of(gu)) * -0.693147181f;
-            bad[q] = false;
+            const float2 uu = mul2(u_of2(gg.x, gg.z), u_of2(gg.y, gg.w));
+            const float2 g = mul2(make_float2(lg2_approx(uu.x), lg2_approx(uu.y)),
+                                  splat2(-kLn2));
+            gq[q0] = g.x;
+            gq[q1] = g.y;
+            bad[q0] = bad[q1] = false;
           } else {
-            bad[q] = !gamma_mt_try(ch.mix_d, ch.mix_c, gn, gu, &g);
+            float2 g;
+            bool o0, o1;
+            gamma_mt_try2(ch.mix_d, ch.mix_c, gg.x, gg.z, gg.y, gg.w, &g, &o0, &o1);
+            gq[q0] = g.x;
+            gq[q1] = g.y;
+            bad[q0] = !o0;
+            bad[q1] = !o1;
           }
-          gq[q] = g;
         }
         const bool rare = (fmaxf(fmaxf(aq[0], aq[1]), fmaxf(aq[2], aq[3])) > kATail) |
                           bad[0] | bad[1] | bad[2] | bad[3];

@@ -45,6 +45,7 @@ constexpr float kNdtD3 = 2.0855841983e+00f;
 constexpr float kNdtD4 = 1.1873321670e-01f;
 // END-COEFFICIENTS
 constexpr float kLog2eHalfNeg = -0.72134752044448170f;  // -log2(e) / 2
+constexpr float kLn2 = 0.693147181f;
 
 // MUFU approximations through documented PTX (ex2 / lg2 / rcp / rsqrt
 // .approx, flush-to-zero): one instruction each, errors of a few ulp.

@@ -37,6 +37,13 @@ namespace bsg {
 namespace {
 
 constexpr int kPredSub = 128;  // voxels staged per pass (one per thread)
+// Resident blocks per SM asked of ptxas: 12 (40 registers, full occupancy;
+// measured faster than the 52-register schedule at 9 blocks) while the
+// design row and the group sums fit, fewer for larger P and S.
+template <int P, int S>
+constexpr int pred_min_blocks() {
+  return (P <= 5 && S <= 2) ? 12 : (P + S <= 8 ? 10 : 8);
+}
 static_assert(kPredSub == kPredThreads, "staging uses one voxel per thread");
 
 // A&S 26.2.17 with 1/sqrt(2 pi) folded in: c * (b1 t + ... + b5 t^5).
@@ -50,21 +57,49 @@ constexpr float kA5 = 0.39894228f * 1.330274429f;
 // flipped when Y = 0: the observed outcome lies on the tail side iff a < 0.
 // Tail side: log2(c t poly(t)) - eta^2 / (2 ln 2); other side:
 // log2(1 - c t poly(t) exp(-eta^2 / 2)).
+// Products and sums carry explicit rounding, so the f32x2 forms below give
+// exactly the scalar values per component.
 __device__ __forceinline__ float log2lik_as(float a) {
   const float t = rcp_approx(fmaf(0.2316419f, fabsf(a), 1.0f));
-  const float r = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, kA5, kA4), kA3), kA2), kA1);
-  const float w = (a * -0.721347520f) * a;  // -eta^2 / 2 in log2 units
+  const float r =
+      __fmul_rn(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, kA5, kA4), kA3), kA2), kA1));
+  const float w = __fmul_rn(__fmul_rn(a, -0.721347520f), a);  // -eta^2/2, log2 units
   const bool tail = a < 0.f;
   const float u = tail ? r : fmaf(-r, ex2_approx(w), 1.0f);
-  return lg2_approx(u) + (tail ? w : 0.f);
+  return __fadd_rn(lg2_approx(u), tail ? w : 0.f);
 }
 
-// log2 P(Y | eta) for the t/logit links, P(Y = 1) = 1 / (1 + exp(-z)) with
+__device__ __forceinline__ float2 log2lik_as2(float2 a) {
+  const float2 h = fma2(splat2(0.2316419f), make_float2(fabsf(a.x), fabsf(a.y)), splat2(1.0f));
+  const float2 t = make_float2(rcp_approx(h.x), rcp_approx(h.y));
+  const float2 r = mul2(t, fma2(t, fma2(t, fma2(t, fma2(t, splat2(kA5), splat2(kA4)),
+                                                splat2(kA3)), splat2(kA2)), splat2(kA1)));
+  const float2 w = mul2(mul2(a, splat2(-0.721347520f)), a);
+  const float2 fm = fma2(mul2(r, splat2(-1.f)),
+                         make_float2(ex2_approx(w.x), ex2_approx(w.y)), splat2(1.0f));
+  const bool t0 = a.x < 0.f, t1 = a.y < 0.f;
+  return add2(make_float2(lg2_approx(t0 ? r.x : fm.x), lg2_approx(t1 ? r.y : fm.y)),
+              make_float2(t0 ? w.x : 0.f, t1 ? w.y : 0.f));
+}
+
+// -log2 P(Y | eta) for the t/logit links, P(Y = 1) = 1 / (1 + exp(-z)) with
 // z = eta / lf (ProbLogitGPU_prediction, covarGPU.cu:1750-1781), for a = z
-// with its sign flipped when Y = 0: -log2(1 + exp(-a)).
-__device__ __forceinline__ float log2lik_logit(float a) {
-  const float e = ex2_approx(fabsf(a) * -1.44269504f);
-  return -(lg2_approx(1.f + e) + fmaxf(-a, 0.f) * 1.44269504f);
+// with its sign flipped when Y = 0: log2(1 + exp(-a)) (the sums subtract it).
+__device__ __forceinline__ float nlog2lik_logit(float a) {
+  const float e = ex2_approx(__fmul_rn(fabsf(a), -1.44269504f));
+  return fmaf(fmaxf(-a, 0.f), 1.44269504f, lg2_approx(__fadd_rn(1.f, e)));
+}
+
+__device__ __forceinline__ float2 nlog2lik_logit2(float2 a) {
+  const float2 s = mul2(make_float2(fabsf(a.x), fabsf(a.y)), splat2(-1.44269504f));
+  const float2 e1 = add2(splat2(1.f), make_float2(ex2_approx(s.x), ex2_approx(s.y)));
+  return fma2(make_float2(fmaxf(-a.x, 0.f), fmaxf(-a.y, 0.f)), splat2(1.44269504f),
+              make_float2(lg2_approx(e1.x), lg2_approx(e1.y)));
+}
+
+__device__ __forceinline__ float2 sign_flip2(float2 a, uint32_t m0, uint32_t m1) {
+  return make_float2(__uint_as_float(__float_as_uint(a.x) ^ m0),
+                     __uint_as_float(__float_as_uint(a.y) ^ m1));
 }
 
 __device__ __forceinline__ bool predict_gate(const ChainDev &ch, int mode) {
@@ -73,13 +108,15 @@ __device__ __forceinline__ bool predict_gate(const ChainDev &ch, int mode) {
   return s > ch.burnin && (s % (ch.thin > 0 ? ch.thin : 1)) == 0;
 }
 
-// P covariates, the first S of them group columns.  Shared row per voxel:
-// P coefficients then beta_WM WM_v, padded to float4s.
+// P covariates, the first S of them group columns.  Voxels are staged in
+// pairs: pair row u holds (b_2u,p, b_2u+1,p) for p = 0..P (the P
+// coefficients, then beta_WM WM_v), padded to float4s, so that each thread
+// evaluates two voxels per f32x2 operation.
 template <int P, int S>
-__global__ void __launch_bounds__(kPredThreads)
+__global__ void __launch_bounds__(kPredThreads, pred_min_blocks<P, S>())
     predict_kernel(const DatasetDev *__restrict__ dsv, ChainDev *__restrict__ chv,
                    const BlockMap *__restrict__ map, int chain, int mode) {
-  constexpr int Q = (P + 1 + 3) / 4;  // float4s per staged voxel
+  constexpr int R2 = (2 * (P + 1) + 3) / 4;  // float4s per staged voxel pair
   // Coefficients of this sweep are final once the previous kernel is done.
   cudaGridDependencySynchronize();
   cudaTriggerProgrammaticLaunchCompletion();
@@ -97,12 +134,15 @@ __global__ void __launch_bounds__(kPredThreads)
   const int word = i0 / 32 + warp;  // this warp's 32-subject outcome word
   const int tw = ch.pred_tile;      // voxels per tile
 
-  __shared__ float4 Bs[kPredSub][Q];
+  __shared__ float4 Bs2[kPredSub / 2][R2];
   __shared__ uint32_t Ys[kPredThreads / 32][kPredSub];
 
-  float x[P];
+  float2 xx[P];  // the subject's design row, duplicated for f32x2 operands
 #pragma unroll
-  for (int p = 0; p < P; ++p) x[p] = i < N ? d.covar[(size_t)p * N + i] : 0.f;
+  for (int p = 0; p < P; ++p) {
+    const float xv = i < N ? d.covar[(size_t)p * N + i] : 0.f;
+    xx[p] = make_float2(xv, xv);
+  }
   double acc[S];
 #pragma unroll
   for (int g = 0; g < S; ++g) acc[g] = 0.0;
@@ -122,19 +162,12 @@ __global__ void __launch_bounds__(kPredThreads)
       const int pos = q0 + tid;
       const int c = pos < n0 ? 0 : 1, j = c ? pos - n0 : pos;
       const int sc = d.nb[c][j], v = d.vidx[c][j];
-      float b[4 * Q];
+      float *row = reinterpret_cast<float *>(&Bs2[tid >> 1][0]) + (tid & 1);
 #pragma unroll
-      for (int p = 0; p < 4 * Q; ++p) {
-        if (p < P)
-          b[p] = de ? (float)(ch.acc_sum[(size_t)p * V + v] * inv_nk)
-                    : ch.beta[(size_t)p * Vp + sc];
-        else
-          b[p] = 0.f;
-      }
-      b[P] = bwc * (d.wm ? d.wm[v] : 1.f);
-#pragma unroll
-      for (int u = 0; u < Q; ++u)
-        Bs[tid][u] = make_float4(b[4 * u], b[4 * u + 1], b[4 * u + 2], b[4 * u + 3]);
+      for (int p = 0; p < P; ++p)
+        row[2 * p] = de ? (float)(ch.acc_sum[(size_t)p * V + v] * inv_nk)
+                        : ch.beta[(size_t)p * Vp + sc];
+      row[2 * P] = bwc * (d.wm ? d.wm[v] : 1.f);
     }
     if (word < d.W) {
       for (int k = lane; k < nsub; k += 32) {
@@ -148,38 +181,67 @@ __global__ void __launch_bounds__(kPredThreads)
       const int sh = 31 - lane;  // brings this subject's bit to the sign
       for (int k0 = 0; k0 < nsub; k0 += 32) {
         const int k1 = min(k0 + 32, nsub);
-        float s32[S];
+        float2 s2[S];  // FP32 sums of the even (.x) and odd (.y) voxels
 #pragma unroll
-        for (int g = 0; g < S; ++g) s32[g] = 0.f;
+        for (int g = 0; g < S; ++g) s2[g] = make_float2(0.f, 0.f);
+        // voxels k, k + 1 of one pair row, then an odd last voxel alone from
+        // the .x halves
+        int k = k0;
 #pragma unroll 2
-        for (int k = k0; k < k1; ++k) {
-          float b[4 * Q];
+        for (; k + 1 < k1; k += 2) {
+          float2 bp[2 * R2];
 #pragma unroll
-          for (int u = 0; u < Q; ++u) {
-            const float4 f = Bs[k][u];
-            b[4 * u] = f.x, b[4 * u + 1] = f.y, b[4 * u + 2] = f.z, b[4 * u + 3] = f.w;
+          for (int u = 0; u < R2; ++u) {
+            const float4 f = Bs2[k >> 1][u];
+            bp[2 * u] = make_float2(f.x, f.y);
+            bp[2 * u + 1] = make_float2(f.z, f.w);
           }
-          // sign mask: flips eta's sign when Y = 0
-          const uint32_t ymask = ~(Ys[warp][k] << sh) & 0x80000000u;
+          const uint2 yy = *reinterpret_cast<const uint2 *>(&Ys[warp][k]);
+          // sign masks: flip eta's sign when Y = 0
+          const uint32_t m0 = ~(yy.x << sh) & 0x80000000u, m1 = ~(yy.y << sh) & 0x80000000u;
           if (de) {
-            float eta = b[P];
+            float2 eta = bp[P];
 #pragma unroll
-            for (int p = 0; p < P; ++p) eta = fmaf(b[p], x[p], eta);
-            const float a = __uint_as_float(__float_as_uint(eta) ^ ymask);
-            s32[0] += logit ? log2lik_logit(a) : log2lik_as(a);
+            for (int p = 0; p < P; ++p) eta = fma2(bp[p], xx[p], eta);
+            const float2 a = sign_flip2(eta, m0, m1);
+            s2[0] = logit ? sub2(s2[0], nlog2lik_logit2(a)) : add2(s2[0], log2lik_as2(a));
           } else {
-            float rest = b[P];
+            float2 rest = bp[P];
 #pragma unroll
-            for (int p = S; p < P; ++p) rest = fmaf(b[p], x[p], rest);
+            for (int p = S; p < P; ++p) rest = fma2(bp[p], xx[p], rest);
 #pragma unroll
             for (int g = 0; g < S; ++g) {
-              const float a = __uint_as_float(__float_as_uint(b[g] + rest) ^ ymask);
-              s32[g] += logit ? log2lik_logit(a * ilf) : log2lik_as(a);
+              const float2 a = sign_flip2(add2(bp[g], rest), m0, m1);
+              s2[g] = logit ? sub2(s2[g], nlog2lik_logit2(mul2(a, splat2(ilf))))
+                            : add2(s2[g], log2lik_as2(a));
+            }
+          }
+        }
+        if (k < k1) {
+          const float *br = reinterpret_cast<const float *>(&Bs2[k >> 1][0]);
+          const uint32_t m0 = ~(Ys[warp][k] << sh) & 0x80000000u;
+          if (de) {
+            float eta = br[2 * P];
+#pragma unroll
+            for (int p = 0; p < P; ++p) eta = fmaf(br[2 * p], xx[p].x, eta);
+            const float a = __uint_as_float(__float_as_uint(eta) ^ m0);
+            s2[0].x = logit ? __fsub_rn(s2[0].x, nlog2lik_logit(a))
+                            : __fadd_rn(s2[0].x, log2lik_as(a));
+          } else {
+            float rest = br[2 * P];
+#pragma unroll
+            for (int p = S; p < P; ++p) rest = fmaf(br[2 * p], xx[p].x, rest);
+#pragma unroll
+            for (int g = 0; g < S; ++g) {
+              const float a = __uint_as_float(__float_as_uint(__fadd_rn(br[2 * g], rest)) ^ m0);
+              s2[g].x = logit ? __fsub_rn(s2[g].x, nlog2lik_logit(__fmul_rn(a, ilf)))
+                              : __fadd_rn(s2[g].x, log2lik_as(a));
             }
           }
         }
 #pragma unroll
-        for (int g = 0; g < S; ++g) acc[g] = fma((double)s32[g], 0.6931471805599453, acc[g]);
+        for (int g = 0; g < S; ++g)
+          acc[g] = fma((double)(s2[g].x + s2[g].y), 0.6931471805599453, acc[g]);
       }
     }
   }
@@ -215,44 +277,46 @@ __global__ void __launch_bounds__(kPredWarps * 32)
 #pragma unroll
     for (int g = 0; g < kMaxP; ++g) {
       double s = 0.0;
-      if (g < G)
+      if (g < G) {
+        // four loads in flight per lane; the sum keeps tile order
+#pragma unroll 4
         for (int t = lane; t < T; t += 32) s += ch.pred_part[((size_t)t * N + i) * G + g];
+      }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
       m[g] = s;
     }
-    if (lane == 0) {
-      if (mode == kPredDE) {
-        ch.pred_subj[i] = m[0];
-      } else {
-        // the subject's own group: the first nonzero group column
-        // (covarGPU.cu:1929-1935)
-        int sub = 0;
-        for (int g = S - 1; g >= 0; --g)
-          if (d.covar[(size_t)g * N + i] != 0.f) sub = g;
-        double own = m[0];
+    if (mode == kPredDE) {
+      if (lane == 0) ch.pred_subj[i] = m[0];
+    } else {
+      // the subject's own group: the first nonzero group column
+      // (covarGPU.cu:1929-1935)
+      int sub = 0;
+      for (int g = S - 1; g >= 0; --g)
+        if (d.covar[(size_t)g * N + i] != 0.f) sub = g;
+      double own = m[0], mg = m[0];
 #pragma unroll
-        for (int g = 0; g < kMaxP; ++g)
-          if (g == sub) own = m[g];
-#pragma unroll
-        for (int g = 0; g < kMaxP; ++g)
-          if (g < S) ch.mpred[(size_t)i * S + g] = m[g];
+      for (int g = 0; g < kMaxP; ++g) {
+        if (g == sub) own = m[g];
+        if (g == lane) mg = m[g];
+      }
+      if (lane == 0 && mode == kPredKept) ch.pred_subj[i] = own;
+      // lane g < S stores column g and updates its Qhat entry
+      // (covarGPU.cu:1937-1953): log-sum over kept sweeps of Mpredict[g] -
+      // Mpredict[own]; on the first kept sweep column 0 is set and the
+      // others are log-added onto 0
+      if (lane < S) {
+        ch.mpred[(size_t)i * S + lane] = mg;
         if (mode == kPredKept) {
-          ch.pred_subj[i] = own;
-          // Qhat (covarGPU.cu:1937-1953): log-sum over kept sweeps of
-          // Mpredict[g] - Mpredict[own]; on the first kept sweep column 0
-          // is set and the others are log-added onto 0.
-#pragma unroll
-          for (int g = 0; g < kMaxP; ++g) {
-            if (g >= S) continue;
-            double *q = ch.qhat + (size_t)i * S + g;
-            const double dg = m[g] - own;
-            if (first && g == 0) {
-              *q = dg;
-            } else {
-              const double mx = fmax(dg, *q);
-              *q = log(exp(*q - mx) + exp(dg - mx)) + mx;
-            }
+          double *q = ch.qhat + (size_t)i * S + lane;
+          const double dg = mg - own;
+          if (first && lane == 0) {
+            *q = dg;
+          } else {
+            // log(exp(q - mx) + exp(dg - mx)) + mx with mx = max(q, dg): one
+            // of the two terms is exp(0) = 1 exactly
+            const double mx = fmax(dg, *q), lo = fmin(dg, *q);
+            *q = log(1.0 + exp(lo - mx)) + mx;
           }
         }
       }

@@ -44,10 +44,10 @@ L2_FLUSH_BYTES = 512 << 20
 CPU_SAMPLE_VOX = 3000   # voxels per colour per thread in a CPU baseline step
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one colour
 # launch of the fused kernel on the brain-sized workload, the mean of the
-# colour-0 and colour-1 launches of one ncu capture (44.27 + 0.10 MB and
-# 44.35 + 0.11 MB).  ncu cannot run inside a timed bench, so the captured
+# colour-0 and colour-1 launches of one ncu capture (43.81 + 0.08 MB and
+# 43.89 + 0.09 MB).  ncu cannot run inside a timed bench, so the captured
 # figure is carried here and reported only for that workload.
-NCU_TRAFFIC_PER_LAUNCH = 44.415e6
+NCU_TRAFFIC_PER_LAUNCH = 43.935e6
 
 
 def fused_flops_per_update(P: int) -> int:

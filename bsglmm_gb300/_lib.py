@@ -63,6 +63,7 @@ SIGNATURES = {
     "bsg_get_dic": (_i32, [_P, _i32, _P]),
     "bsg_sweep_supplied": (_i32, [_P, _i32, _P, _P, _P, _P, _i32]),
     "bsg_fp32_peak": (_i32, [_i32, C.POINTER(C.c_double)]),
+    "bsg_selftest_pairs": (_i32, [_i32, C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]),
     "bsg_checkpoint_size": (_i64, [_P, _i32]),
     "bsg_checkpoint": (_i32, [_P, _i32, _P, _i64]),
     "bsg_restore": (_i32, [_P, _i32, _P, _i64]),

@@ -30,6 +30,7 @@
 // other side log(1 - c t poly(t) exp(-eta^2 / 2)).  The reference's FP32
 // y log(p + 1e-35) + (1 - y) log(1 - p + 1e-35) is the same quantity where
 // its 1 - p does not cancel (|eta| below about 5).
+#include "../../include/bsglmm_gb300.h"
 #include "bsg_device.cuh"
 
 namespace bsg {
@@ -419,6 +420,41 @@ struct OccF {
   static int fail() { return 1; }
 };
 
+// Self-check of the f32x2 forms: for n random inputs, each paired helper
+// against two calls of its scalar form, compared bit for bit (and the
+// Marsaglia-Tsang acceptance decisions); mismatches are counted.
+__global__ void pairs_selftest_kernel(int64_t n, uint32_t k0, uint32_t k1,
+                                      unsigned long long *bad) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint4 r = philox1(make_uint4((uint32_t)i, (uint32_t)(i >> 32), 0u, 0xA5u), k0, k1);
+  const uint4 q = philox1(make_uint4((uint32_t)i, (uint32_t)(i >> 32), 1u, 0xA5u), k0, k1);
+  auto ne = [](float x, float y) { return __float_as_uint(x) != __float_as_uint(y); };
+  // arguments over [-8, 8): both inversion branches, the clamp and both
+  // log-likelihood sides
+  const float a0 = fmaf(u_of(r.x), 16.f, -8.f), a1 = fmaf(u_of(r.y), 16.f, -8.f);
+  unsigned m = 0;
+  const float c0 = fminf(a0, kATail), c1 = fminf(a1, kATail);
+  const float2 t = tn_lower_inv2(make_float2(c0, c1), r.z, r.w);
+  m += ne(t.x, tn_lower_inv(c0, r.z)) + ne(t.y, tn_lower_inv(c1, r.w));
+  const float2 z = normal_of2(q.x, q.y);
+  m += ne(z.x, normal_of(q.x)) + ne(z.y, normal_of(q.y));
+  // Gamma(4.5): the t_8 weights of the logistic link
+  const float dd = 4.5f - 1.f / 3.f, cc = rsqrtf(9.f * dd);
+  float2 g;
+  bool o0, o1;
+  gamma_mt_try2(dd, cc, q.x, q.z, q.y, q.w, &g, &o0, &o1);
+  float g0, g1;
+  const bool s0 = gamma_mt_try(dd, cc, q.x, q.y, &g0);
+  const bool s1 = gamma_mt_try(dd, cc, q.z, q.w, &g1);
+  m += ne(g.x, g0) + ne(g.y, g1) + (o0 != s0) + (o1 != s1);
+  const float2 la = log2lik_as2(make_float2(a0, a1));
+  m += ne(la.x, log2lik_as(a0)) + ne(la.y, log2lik_as(a1));
+  const float2 ll = nlog2lik_logit2(make_float2(a0, a1));
+  m += ne(ll.x, nlog2lik_logit(a0)) + ne(ll.y, nlog2lik_logit(a1));
+  if (m) atomicAdd(bad, (unsigned long long)m);
+}
+
 }  // namespace
 
 cudaError_t launch_predict(int P, int S, const DatasetDev *ds, ChainDev *ch,
@@ -446,3 +482,26 @@ cudaError_t launch_predict_finish(const DatasetDev *ds, ChainDev *ch,
 }
 
 }  // namespace bsg
+
+extern "C" bsg_status bsg_selftest_pairs(int32_t device, int64_t n, uint64_t seed,
+                                         int64_t *mismatches) {
+  if (!mismatches || n < 0) return BSG_ERR_INVALID;
+  int nd = 0;
+  if (cudaGetDeviceCount(&nd) != cudaSuccess || nd == 0) return BSG_ERR_NO_DEVICE;
+  if (cudaSetDevice(device) != cudaSuccess) return BSG_ERR_INVALID;
+  unsigned long long *bad = nullptr;
+  if (cudaMalloc(&bad, sizeof(*bad)) != cudaSuccess) return BSG_ERR_CUDA;
+  unsigned long long h = 0;
+  cudaError_t e = cudaMemset(bad, 0, sizeof(*bad));
+  if (e == cudaSuccess && n > 0) {
+    const int threads = 256;
+    bsg::pairs_selftest_kernel<<<(unsigned)((n + threads - 1) / threads), threads>>>(
+        n, (uint32_t)seed, (uint32_t)(seed >> 32), bad);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(&h, bad, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(bad);
+  if (e != cudaSuccess) return BSG_ERR_CUDA;
+  *mismatches = (int64_t)h;
+  return BSG_OK;
+}

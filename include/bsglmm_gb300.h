@@ -263,6 +263,13 @@ bsg_status bsg_omega_update_noalloc(const float *spatcoef, const int32_t *vox,
  * counterpart in the reference. */
 bsg_status bsg_fp32_peak(int32_t device, double *tflops);
 
+/* Self-check of the paired (f32x2) forms of the latent-draw, gamma and
+ * log-likelihood helpers against their scalar forms on n seeded random
+ * inputs, compared bit for bit; *mismatches receives the count (0 when the
+ * two forms agree).  No counterpart in the reference. */
+bsg_status bsg_selftest_pairs(int32_t device, int64_t n, uint64_t seed,
+                              int64_t *mismatches);
+
 #ifdef __cplusplus
 }
 #endif

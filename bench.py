@@ -16,7 +16,10 @@ column means back (covarGPU.cu:582,1106-1108).  With N > 1 (torchrun) every
 rank runs an independent chain on its own GPU (replicas, weak scaling).
 `--impl reference` times the reference's CPU sweep (the oracle's timing port
 of covar.cpp's updateZ / updateSpatCoef / updateSpatCoefPrec) on all host
-cores.
+cores, one chain per core; each step is a bounded sample of the study (the
+first voxels of each colour), sized so that the timed steps take about
+90 s in all.  The `cpu_baseline` of the GPU arm is one such sample of about
+10 s.
 """
 from __future__ import annotations
 
@@ -41,7 +44,9 @@ UNIT = "subject-voxel updates/s"
 WORKLOAD = "brain-sized plain FP32 GPU form: 91x109x91 grid, ellipsoid mask, N=1000, P=5"
 C_TN = 40          # FP32 flops of one truncated-normal draw's accept path
 L2_FLUSH_BYTES = 512 << 20
-CPU_SAMPLE_VOX = 3000   # voxels per colour per thread in a CPU baseline step
+CPU_CAL_VOX = 2000      # voxels per colour of the CPU calibration sweep
+CPU_BASELINE_S = 10.0   # seconds of CPU work in the cpu_baseline sample
+CPU_REFERENCE_S = 90.0  # seconds of CPU work in a whole reference-arm run
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one colour
 # launch of the fused kernel on the brain-sized workload, the mean of the
 # colour-0 and colour-1 launches of one ncu capture (43.81 + 0.08 MB and
@@ -139,22 +144,24 @@ def measured_peaks():
 
 
 # ------------------------------------------------------------ CPU legs ---
-def cpu_port_rate(study, threads: int, steps: int, warmup: int, nvox: int):
+def cpu_port_rate(study, threads: int, steps: int, warmup: int, target_s: float):
     """The oracle's timing port of the reference CPU sweep, one independent
-    chain per thread, each step restricted to `nvox` voxels per colour."""
+    chain per thread.  A short calibration sweep sizes each step to about
+    `target_s` seconds: a step sweeps the first `nvox` voxels of each colour,
+    up to the whole study.  `warmup` (at least one) untimed steps of that
+    size precede the `steps` timed ones."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
     oracle.build_oracle()
     pb = oracle.Problem(study.mask, study.covar, study.data, study.nsubtypes)
     ports = [oracle.Port(pb, seed=1000 + t) for t in range(threads)]
-    upd = ports[0].updates(nvox)
+    ncmax = max(pb.n0, pb.n1)
 
-    def work(pt, n):
-        for _ in range(n):
-            pt.sweep(nvox)
-
-    def run(n):
-        ts = [threading.Thread(target=work, args=(pt, n)) for pt in ports]
+    def run(n, nvox):
+        def work(pt):
+            for _ in range(n):
+                pt.sweep(nvox)
+        ts = [threading.Thread(target=work, args=(pt,)) for pt in ports]
         t0 = time.perf_counter()
         for t in ts:
             t.start()
@@ -162,13 +169,20 @@ def cpu_port_rate(study, threads: int, steps: int, warmup: int, nvox: int):
             t.join()
         return time.perf_counter() - t0
 
-    if warmup:
-        run(warmup)
-    dt = run(steps)
+    cal = min(CPU_CAL_VOX, ncmax)
+    run(1, cal)  # first touch of the chains' state
+    dt = run(1, cal)
+    nvox = int(min(ncmax, max(cal, cal * target_s / max(dt, 1e-6))))
+    upd = ports[0].updates(nvox)
+    for _ in range(max(warmup, 1)):
+        run(1, nvox)
+    dt = run(steps, nvox)
     rate = upd * threads * steps / dt
-    sample = (f"{steps} sweep(s) per thread restricted to the first {nvox} voxels "
-              f"of each colour ({upd} subject-voxel updates per sweep), "
-              f"{threads} independent chains")
+    what = ("the whole study" if nvox >= ncmax else
+            f"the first {nvox} voxels of each colour")
+    sample = (f"{steps} sweep(s) per thread over {what} ({upd} subject-voxel "
+              f"updates per sweep, {dt / steps:.1f} s per step), {threads} "
+              f"independent chains")
     return rate, dt / steps, sample
 
 
@@ -179,8 +193,11 @@ def run_reference(args, rank, world):
     from bsglmm_gb300 import synth
     study = synth.config1(seed=1)
     threads = os.cpu_count() or 1
+    # each step a bounded sample, so that the whole --steps/--warmup run
+    # stays within a couple of minutes
+    per_step = min(10.0, max(0.25, CPU_REFERENCE_S / max(args.steps, 1)))
     rate, sec_per_step, sample = cpu_port_rate(study, threads, args.steps,
-                                               args.warmup, CPU_SAMPLE_VOX)
+                                               args.warmup, per_step)
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -297,7 +314,7 @@ def run_ours(args, rank, world, local):
     cpu = None
     if world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        crate, _, sample = cpu_port_rate(study, threads, 1, 0, CPU_SAMPLE_VOX)
+        crate, _, sample = cpu_port_rate(study, threads, 1, 1, CPU_BASELINE_S)
         cpu = {"value": crate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": sample}
     peaks = measured_peaks()

@@ -251,9 +251,10 @@ std::string status_text(int bits) {
 
 constexpr int kParityThreads = 128;  // tile of the supplied-variate sweep
 
-// Partial rows of the colour kernels, one per block of a chain: column sums
-// (colour 0) and pairs + column sums (colour 1), sized for the smallest
-// tile the context launches.
+// Partials of the colour kernels, one per block of a chain and value
+// (value-major, so that the last block's sums read consecutive blocks):
+// column sums (colour 0) and pairs + column sums (colour 1), sized for the
+// smallest tile the context launches; tot0 takes colour 0's totals.
 bsg_status ensure_partials(bsg_ctx *ctx, int vpb) {
   cudaError_t e;
   for (auto &c : ctx->ch) {
@@ -272,6 +273,13 @@ bsg_status ensure_partials(bsg_ctx *ctx, int vpb) {
       CK(e);
       c.cap1 = n1;
     }
+    if (!c.dev.tot0) {
+      c.dev.tot0 = (double *)dalloc(ctx, sizeof(double) * kP0Vals, &e);
+      CK(e);
+      CK(cudaMemsetAsync(c.dev.tot0, 0, sizeof(double) * kP0Vals, ctx->stream));
+    }
+    c.dev.pstride0 = (int32_t)c.cap0;
+    c.dev.pstride1 = (int32_t)c.cap1;
   }
   return BSG_OK;
 }

@@ -23,16 +23,17 @@
 
 namespace bsg {
 
-// Resident 256-thread blocks per SM asked of ptxas: three (85 registers) up
-// to P = 5, two (128 registers) above, measured fastest on the brain-sized
-// study; BSG_FUSED_MIN_BLOCKS overrides it for tuning builds.
+// Resident 256-thread blocks per SM asked of ptxas: three (80 registers) up
+// to P = 6, two (128 registers) above, measured fastest on the brain-sized
+// study (P = 5) and the 1.5M-voxel study (P = 6, 2.16 -> 2.11 ms per sweep
+// against two blocks); BSG_FUSED_MIN_BLOCKS overrides it for tuning builds.
 template <int P, bool MIX = false>
 constexpr int fused_min_blocks() {
 #ifdef BSG_FUSED_MIN_BLOCKS
   return BSG_FUSED_MIN_BLOCKS;
 #else
   // the t/logit kernel also keeps the voxel's X' Phi X in registers
-  return MIX ? (P <= 5 ? 2 : 1) : (P <= 5 ? 3 : 2);
+  return MIX ? (P <= 5 ? 2 : 1) : (P <= 6 ? 3 : 2);
 #endif
 }
 
@@ -683,80 +684,107 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
   const int lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
   constexpr int kColOff = kMaxPairs;
   constexpr int NV = NT + P + (WMU ? 1 : 0);  // values reduced per block
+  // The pair products and coefficients of a warp's 32 voxels are summed in
+  // FP32 by a fixed shuffle tree (this part's FP64 pipe does two lanes per
+  // clock per SM: an FP64 tree over all 24 resident warps took about 15 us
+  // per colour-1 launch), then in FP64 across warps and blocks; the beta_WM
+  // term stays FP64 throughout.
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
     if (colour == 0 && q < NT) continue;
-    double val = q < NT ? (double)pv[q] : (q < NT + P ? (double)bnew[q - NT] : wmt);
+    double val;
+    if (q < NT + P) {
+      float f = q < NT ? pv[q] : bnew[q - NT];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+      for (int o = 16; o > 0; o >>= 1) f += __shfl_xor_sync(0xffffffffu, f, o);
+      val = (double)f;
+    } else {
+      val = wmt;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+    }
     if (lane == 0)
       red[warp][q < NT ? q : (q < NT + P ? kColOff + (q - NT) : kWmOff)] = val;
   }
   __syncthreads();
   const int vpb = blockDim.x / LPV;
   const int lb = bm.start / vpb;
+  const int nblk = max(1, (nc + vpb - 1) / vpb);  // blocks of this colour
+  // Sum of one value over the blocks' partials (value-major, so a warp
+  // reads consecutive blocks) in a fixed order, so the draw is bitwise
+  // reproducible: lane l loads the blocks l, l + 32, ... of a 512-block
+  // chunk together and adds them as a tree, then the lanes are combined.
+  auto rows = [&](const double *base, int nrow) -> double {
+    double s = 0.0;
+    for (int c0 = 0; c0 < nrow; c0 += 512) {
+      double v[16];
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        const int r = c0 + lane + 32 * u;
+        v[u] = r < nrow ? __ldcg(base + r) : 0.0;
+      }
+#pragma unroll
+      for (int w = 8; w > 0; w >>= 1)
+#pragma unroll
+        for (int u = 0; u < w; ++u) v[u] += v[u + w];
+      s += v[0];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    return s;
+  };
   if (colour == 0) {
     if (tid < P || (WMU && tid == kMaxP)) {
       const int q = tid < P ? kColOff + tid : kWmOff;
       double s = 0.0;
       for (int w = 0; w < nwarp; ++w) s += red[w][q];
-      ch.partials0[(size_t)lb * kP0Vals + tid] = s;
+      ch.partials0[(size_t)tid * ch.pstride0 + lb] = s;
       __threadfence();
     }
     __syncthreads();
-    if (tid == 0) {  // the last colour-0 block advances this colour's count
-      const int nblk0 = max(1, (nc + vpb - 1) / vpb);
-      if (atomicAdd(ch.done, 1u) == (unsigned)(nblk0 - 1)) {
-        ch.sweep[0] = sweep_ll + 1;
-        ch.done[0] = 0u;
-        __threadfence();
-      }
+    if (tid == 0) is_last = atomicAdd(ch.done, 1u) == (unsigned)(nblk - 1);
+    __syncthreads();
+    if (!is_last) return;
+    // The last colour-0 block sums the column sums (and the beta_WM term)
+    // over the colour's blocks while colour 1 starts, and advances this
+    // colour's count.
+    __threadfence();
+    for (int m = warp; m < P + (WMU ? 1 : 0); m += nwarp) {
+      const int q = m < P ? m : kMaxP;
+      const double s = rows(ch.partials0 + (size_t)q * ch.pstride0, nblk);
+      if (lane == 0) ch.tot0[q] = s;
+    }
+    if (tid == 0) {
+      ch.sweep[0] = sweep_ll + 1;
+      ch.done[0] = 0u;
+      __threadfence();
     }
     return;
   }
   if (tid < kFusedVals) {
     const bool live =
         tid < kMaxPairs ? tid < NT : ((WMU && tid == kWmOff) || (tid - kColOff) < P);
-    double s = 0.0;
-    if (live)
+    if (live) {
+      double s = 0.0;
       for (int w = 0; w < nwarp; ++w) s += red[w][tid];
-    ch.partials1[(size_t)lb * kFusedVals + tid] = s;
-    __threadfence();
+      ch.partials1[(size_t)tid * ch.pstride1 + lb] = s;
+      __threadfence();
+    }
   }
   __syncthreads();
-  const int nblk1 = max(1, (nc + vpb - 1) / vpb);
   if (tid == 0) {
     const unsigned prev = atomicAdd(ch.done + 1, 1u);
-    is_last = prev == (unsigned)(nblk1 - 1);
+    is_last = prev == (unsigned)(nblk - 1);
   }
   __syncthreads();
   if (!is_last) return;
   __threadfence();
-  // Sum the partial rows in a fixed order (so the draw is bitwise
-  // reproducible): warp w takes the live values m = w, w + nwarp, ...; lane
-  // l the rows l, l + 32, ..., in four interleaved sums so that four loads
-  // are in flight, combined in a fixed order and then across lanes.
-  const int n0 = d.n[0];
-  const int nblk0 = max(1, (n0 + vpb - 1) / vpb);
-  auto rows = [&](const double *base, int stride, int nrow) -> double {
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-    int bb = lane;
-    for (; bb + 96 < nrow; bb += 128) {
-      s0 += __ldcg(base + (size_t)bb * stride);
-      s1 += __ldcg(base + (size_t)(bb + 32) * stride);
-      s2 += __ldcg(base + (size_t)(bb + 64) * stride);
-      s3 += __ldcg(base + (size_t)(bb + 96) * stride);
-    }
-    for (; bb < nrow; bb += 32) s0 += __ldcg(base + (size_t)bb * stride);
-    return (s0 + s1) + (s2 + s3);
-  };
+  // warp w takes the live values m = w, w + nwarp, ...; colour 0's totals
+  // (final since that kernel completed) are added to the column sums
   for (int m = warp; m < NV; m += nwarp) {
     const int q = m < NT ? m : (m < NT + P ? kColOff + (m - NT) : kWmOff);
-    double s = rows(ch.partials1 + q, kFusedVals, nblk1);
-    if (q >= kColOff)
-      s += rows(ch.partials0 + (q == kWmOff ? kMaxP : q - kColOff), kP0Vals, nblk0);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    double s = rows(ch.partials1 + (size_t)q * ch.pstride1, nblk);
+    if (q >= kColOff) s += __ldcg(ch.tot0 + (q == kWmOff ? kMaxP : q - kColOff));
     if (lane == 0) tot[q] = s;
   }
   __syncthreads();

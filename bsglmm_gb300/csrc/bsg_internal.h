@@ -94,9 +94,12 @@ struct ChainDev {
   double *acc_sum;         // [P][V]  sum of beta over kept sweeps
   double *acc_sq;          // [P][V]  sum of beta^2
   double *prb_sum;         // [S][V]  sum of the lesion probability
-  double *partials0;       // [colour-0 blocks][kP0Vals] column sums, WM term
-  double *partials1;       // [colour-1 blocks][kFusedVals] pairs, column sums,
-                           // WM term
+  double *partials0;       // [kP0Vals][pstride0] column sums, WM term of
+                           // each colour-0 block (value-major)
+  double *partials1;       // [kFusedVals][pstride1] pairs, column sums, WM
+                           // term of each colour-1 block (value-major)
+  int32_t pstride0, pstride1;  // block rows allocated per value
+  double *tot0;            // [kP0Vals] colour-0 totals of the sweep
   unsigned int *done;      // [2] arrival counters of the colour kernels
   long long *sweep;        // [2] sweeps completed by the colour-c kernel;
                            // sweep[1] is the chain's completed-sweep count

@@ -91,7 +91,9 @@ __device__ double na_gamma(double a, uint32_t slot, const NaArgs &g, int *err) {
     const double x = (double)normal_of(r.x), cx = c * x;
     if (!(cx > -1.0)) continue;
     const double v3 = (1.0 + cx) * (1.0 + cx) * (1.0 + cx);
-    if (log(u_of_d(r.y)) < 0.5 * x * x + dd * (1.0 - v3 + 3.0 * log1p(cx)))
+    const double u = u_of_d(r.y), x2 = x * x;
+    if (u < 1.0 - 0.0331 * x2 * x2 ||  // the squeeze, as the sampler's draw
+        log(u) < 0.5 * x * x + dd * (1.0 - v3 + 3.0 * log1p(cx)))
       return dd * v3 * (boost ? pow(u_of_d(r.z), 1.0 / a) : 1.0);
   }
   *err |= kErrGammaCap;

@@ -10,6 +10,9 @@ namespace bsg {
 // ----------------------------------------------------- FP64 Wishart tail --
 // Marsaglia & Tsang (2000) gamma(a, 1); a < 1 through the U^(1/a) boost.
 // Attempt t of slot uses counter (slot*64 + t, 0, sweep, chain<<8|GAMMA).
+// The squeeze u < 1 - 0.0331 x^4 lies inside the acceptance region, so it
+// accepts exactly the attempts the log test would; it spares the two FP64
+// logarithms in most attempts.
 static __device__ double gamma_mt(double a, uint32_t slot, uint32_t sweep,
                                   uint32_t c3, uint32_t k0, uint32_t k1,
                                   int *err) {
@@ -23,9 +26,10 @@ static __device__ double gamma_mt(double a, uint32_t slot, uint32_t sweep,
     const double cx = c * x;
     if (!(cx > -1.0)) continue;
     const double v3 = (1.0 + cx) * (1.0 + cx) * (1.0 + cx);
-    const double lhs = log(u_of_d(r.y));
-    const double rhs = 0.5 * x * x + dd * (1.0 - v3 + 3.0 * log1p(cx));
-    if (lhs < rhs) return dd * v3 * (boost ? pow(u_of_d(r.z), 1.0 / a) : 1.0);
+    const double u = u_of_d(r.y), x2 = x * x;
+    if (u < 1.0 - 0.0331 * x2 * x2 ||
+        log(u) < 0.5 * x * x + dd * (1.0 - v3 + 3.0 * log1p(cx)))
+      return dd * v3 * (boost ? pow(u_of_d(r.z), 1.0 / a) : 1.0);
   }
   *err |= kErrGammaCap;
   return dd;
@@ -47,12 +51,21 @@ static __device__ void wishart_warp(const ChainDev &ch, const DatasetDev &d,
   const int P = d.P;
   const uint32_t cid = ch.chain_id << 8, sw = (uint32_t)sweep;
   int err = 0;
-  if (lane < P)
-    for (int c = 0; c < P; ++c) {
-      const int r = lane;
-      A[r][c] = (r >= c ? tot[tri(r, c)] : tot[tri(c, r)]) + (r == c ? 1.0 : 0.0);
-      T[r][c] = 0.0;
-    }
+  // entry q of the packed lower triangle is (r, c), r >= c; the lanes take
+  // the entries (one round up to P = 7), so that every stage below is a
+  // few dependent FP64 operations deep (this part's FP64 pipe does two
+  // lanes per clock per SM, so depth, not width, sets the time)
+  auto rc_of = [](int q, int &r, int &c) {
+    r = 0;
+    while ((r + 1) * (r + 2) / 2 <= q) ++r;
+    c = q - r * (r + 1) / 2;
+  };
+  const int NP = P * (P + 1) / 2;
+  for (int q = lane; q < P * P; q += 32) {
+    const int r = q / P, c = q - r * P;
+    A[r][c] = (r >= c ? tot[tri(r, c)] : tot[tri(c, r)]) + (r == c ? 1.0 : 0.0);
+    T[r][c] = 0.0;
+  }
   __syncwarp();
   // S + I = U U' with U upper, last pivot first; U goes to the upper
   // triangle of A (diagonal included), the lower triangle holds the
@@ -69,8 +82,11 @@ static __device__ void wishart_warp(const ChainDev &ch, const DatasetDev &d,
       rd[k] = rs;
     }
     __syncwarp();
-    if (lane < k)
-      for (int j = 0; j <= lane; ++j) A[lane][j] -= A[lane][k] * A[j][k];
+    for (int q = lane; q < k * (k + 1) / 2; q += 32) {
+      int i, j;
+      rc_of(q, i, j);
+      A[i][j] -= A[i][k] * A[j][k];
+    }
     __syncwarp();
   }
   if (ok) {
@@ -115,34 +131,32 @@ static __device__ void wishart_warp(const ChainDev &ch, const DatasetDev &d,
       T[i][j] = z;
     }
     __syncwarp();
-    if (lane < P) {  // row `lane` of B = L T (L lower from Ai)
-      const int i = lane;
-      for (int j = 0; j < P; ++j) {
-        double s = 0.0;
-        for (int k = j; k <= i; ++k) s += Ai[i][k] * T[k][j];
-        B[i][j] = j <= i ? s : 0.0;
-      }
+    for (int q = lane; q < NP; q += 32) {  // B = L T, lower (L from Ai)
+      int i, j;
+      rc_of(q, i, j);
+      double s = 0.0;
+      for (int k = j; k <= i; ++k) s += Ai[i][k] * T[k][j];
+      B[i][j] = s;
     }
     __syncwarp();
     bool fin = true;
-    if (lane < P) {
-      const int i = lane;
-      for (int j = 0; j < P; ++j) {
-        const int K = i < j ? i : j;
-        double s = 0.0;
-        for (int k = 0; k <= K; ++k) s += B[i][k] * B[j][k];
-        A[i][j] = s;  // A is free again
-        fin = fin && isfinite(s);
-      }
+    for (int q = lane; q < NP; q += 32) {  // Omega = B B', both triangles
+      int i, j;
+      rc_of(q, i, j);
+      double s = 0.0;
+      for (int k = 0; k <= j; ++k) s += B[i][k] * B[j][k];
+      A[i][j] = s;  // A is free again
+      A[j][i] = s;
+      fin = fin && isfinite(s);
     }
     fin = __all_sync(0xffffffffu, fin);
     __syncwarp();
     if (fin) {
-      if (lane < P)
-        for (int j = 0; j < P; ++j) {
-          ch.omega_d[lane * P + j] = A[lane][j];
-          ch.omega_f[lane * P + j] = (float)A[lane][j];
-        }
+      for (int q = lane; q < P * P; q += 32) {
+        const int r = q / P, c = q - r * P;
+        ch.omega_d[q] = A[r][c];
+        ch.omega_f[q] = (float)A[r][c];
+      }
     } else {
       err |= kErrNaN;
     }

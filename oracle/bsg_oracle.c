@@ -639,9 +639,11 @@ static double gamma_mt(double a, uint32_t slot, uint32_t sweep,
     double cx = c * x;
     if (!(cx > -1.0)) continue;
     double v3 = (1.0 + cx) * (1.0 + cx) * (1.0 + cx);
-    double lhs = log(orc_u_from_bits(o[1]));
-    double rhs = 0.5 * x * x + d * (1.0 - v3 + 3.0 * log1p(cx));
-    if (lhs < rhs) {
+    double u = orc_u_from_bits(o[1]), x2 = x * x;
+    /* the squeeze u < 1 - 0.0331 x^4 lies inside the acceptance region:
+     * it decides as the log test would, without the logarithms */
+    if (u < 1.0 - 0.0331 * x2 * x2 ||
+        log(u) < 0.5 * x * x + d * (1.0 - v3 + 3.0 * log1p(cx))) {
       if (need_boost) boost = pow(orc_u_from_bits(o[2]), 1.0 / a);
       return d * v3 * boost;
     }

@@ -274,9 +274,11 @@ bsg_status ensure_partials(bsg_ctx *ctx, int vpb) {
       c.cap1 = n1;
     }
     if (!c.dev.tot0) {
-      c.dev.tot0 = (double *)dalloc(ctx, sizeof(double) * kP0Vals, &e);
+      const size_t n = kP0Vals + kMaxP + kMaxPairs;
+      c.dev.tot0 = (double *)dalloc(ctx, sizeof(double) * n, &e);
       CK(e);
-      CK(cudaMemsetAsync(c.dev.tot0, 0, sizeof(double) * kP0Vals, ctx->stream));
+      CK(cudaMemsetAsync(c.dev.tot0, 0, sizeof(double) * n, ctx->stream));
+      c.dev.wdraw = c.dev.tot0 + kP0Vals;
     }
     c.dev.pstride0 = (int32_t)c.cap0;
     c.dev.pstride1 = (int32_t)c.cap1;

@@ -754,6 +754,15 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
       const double s = rows(ch.partials0 + (size_t)q * ch.pstride0, nblk);
       if (lane == 0) ch.tot0[q] = s;
     }
+    // the sweep's Bartlett variates (they do not depend on S), for the
+    // Omega draw at the end of colour 1
+    if (!SUPP && warp == nwarp - 1) {
+      const int e = __reduce_or_sync(0xffffffffu, wishart_draws(ch, d, sweep_ll, lane, ch.wdraw));
+      if (e && lane == 0) {
+        atomicOr(ch.status, e);
+        atomicOr(ch.any_status, e);
+      }
+    }
     if (tid == 0) {
       ch.sweep[0] = sweep_ll + 1;
       ch.done[0] = 0u;

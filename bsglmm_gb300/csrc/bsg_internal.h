@@ -100,6 +100,8 @@ struct ChainDev {
                            // term of each colour-1 block (value-major)
   int32_t pstride0, pstride1;  // block rows allocated per value
   double *tot0;            // [kP0Vals] colour-0 totals of the sweep
+  double *wdraw;           // [kMaxP + kMaxPairs] the sweep's Bartlett variates:
+                           // sqrt(chi^2) diagonal, then the normals
   unsigned int *done;      // [2] arrival counters of the colour kernels
   long long *sweep;        // [2] sweeps completed by the colour-c kernel;
                            // sweep[1] is the chain's completed-sweep count

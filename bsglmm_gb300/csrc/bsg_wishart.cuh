@@ -35,19 +35,41 @@ static __device__ double gamma_mt(double a, uint32_t slot, uint32_t sweep,
   return dd;
 }
 
+// The Bartlett variates of a sweep, which do not depend on S: lane i < P
+// draws sqrt(chi^2(df - i)) into wd[i], lane q < P(P-1)/2 the normal of
+// the q-th strictly lower entry (row-major) into wd[kMaxP + q].  Run by the
+// last colour-0 block, off the Omega draw's dependency chain.  Returns the
+// lane's error bits.
+static __device__ int wishart_draws(const ChainDev &ch, const DatasetDev &d,
+                                    long long sweep, int lane, double *wd) {
+  const int P = d.P;
+  const uint32_t cid = ch.chain_id << 8, sw = (uint32_t)sweep;
+  int err = 0;
+  const double df = (double)d.V + (double)ch.df_offset;
+  if (lane < P)
+    wd[lane] = sqrt(2.0 * gamma_mt(0.5 * (df - lane), (uint32_t)lane, sw,
+                                   cid | kTagGamma, ch.key0, ch.key1, &err));
+  if (lane < P * (P - 1) / 2) {
+    const uint4 r = philox1(make_uint4((uint32_t)(lane >> 2), 0u, sw, cid | kTagWNorm),
+                            ch.key0, ch.key1);
+    wd[kMaxP + lane] = (double)normal_of(pick4(r, lane & 3));
+  }
+  return err;
+}
+
 // Omega | beta ~ Wishart(df, (S + I)^-1) by the Bartlett construction of
 // rwishart2 (cholesky.cpp:245-286), FP64, one warp.  The reference forms
 // chol((S + I)^-1) by chol -> invert -> chol (covar.cpp:286-291,
-// covarGPU.cu:1099-1104); the same factor is reached here with a third of
-// the dependent work: with the reverse (upper) Cholesky S + I = U U', the
-// inverse is U^-T U^-1 and U^-T is lower triangular with a positive
-// diagonal, so chol((S + I)^-1) = U^-T (the Cholesky factor is unique).
+// covarGPU.cu:1099-1104); the same factor is reached here with a fraction
+// of the dependent work: with the reverse (upper) Cholesky S + I = U U',
+// the inverse is U^-T U^-1 and U^-T is lower triangular with a positive
+// diagonal, so chol((S + I)^-1) = U^-T (the Cholesky factor is unique),
+// and B = U^-T T comes from forward substitution without forming U^-T.
 static __device__ void wishart_warp(const ChainDev &ch, const DatasetDev &d,
                                     const double *tot, long long sweep,
                                     bool kept, long long nk, int supplied,
                                     const Supplied &sup, int lane) {
-  __shared__ double A[kMaxP][kMaxP], Ai[kMaxP][kMaxP], T[kMaxP][kMaxP],
-      B[kMaxP][kMaxP], rd[kMaxP];
+  __shared__ double A[kMaxP][kMaxP], T[kMaxP][kMaxP], B[kMaxP][kMaxP], rd[kMaxP];
   const int P = d.P;
   const uint32_t cid = ch.chain_id << 8, sw = (uint32_t)sweep;
   int err = 0;
@@ -90,53 +112,38 @@ static __device__ void wishart_warp(const ChainDev &ch, const DatasetDev &d,
     __syncwarp();
   }
   if (ok) {
-    // column `lane` of W = U^-1 (upper): W[i][j] = -rd[i] sum_{k>i} U[i][k] W[k][j];
-    // the factor L = U^-T = W' goes to Ai (lower)
-    if (lane < P) {
-      const int j = lane;
-      double w[kMaxP];
-      w[j] = rd[j];
-      for (int i = j - 1; i >= 0; --i) {
-        double s = 0.0;
-        for (int k = i + 1; k <= j; ++k) s += A[i][k] * w[k];
-        w[i] = -rd[i] * s;
-      }
-      for (int i = 0; i < P; ++i) Ai[j][i] = i <= j ? w[i] : 0.0;
-    }
-    __syncwarp();
-  }
-  if (ok) {
-    const double df = (double)d.V + (double)ch.df_offset;
-    if (lane < P) {
-      const double c2 = supplied ? sup.chi2[lane]
-                                 : 2.0 * gamma_mt(0.5 * (df - lane), (uint32_t)lane,
-                                                  sw, cid | kTagGamma, ch.key0,
-                                                  ch.key1, &err);
-      T[lane][lane] = sqrt(c2);
-    }
+    // T: the Bartlett factor, lower; sqrt(chi^2) on the diagonal and
+    // normals below it (drawn by the last colour-0 block of this sweep,
+    // or supplied)
     const int nw = P * (P - 1) / 2;
+    if (lane < P) T[lane][lane] = supplied ? sqrt(sup.chi2[lane]) : __ldcg(ch.wdraw + lane);
     if (lane < nw) {
       int i = 1;
       while ((i + 1) * i / 2 <= lane) ++i;  // row i: lane in [i(i-1)/2, i(i+1)/2)
       const int j = lane - i * (i - 1) / 2;
-      double z;
-      if (supplied) {
-        z = sup.wnorm[lane];
-      } else {
-        const uint4 r = philox1(make_uint4((uint32_t)(lane >> 2), 0u, sw,
-                                           cid | kTagWNorm),
-                                ch.key0, ch.key1);
-        z = (double)normal_of(pick4(r, lane & 3));
-      }
-      T[i][j] = z;
+      T[i][j] = supplied ? sup.wnorm[lane] : __ldcg(ch.wdraw + kMaxP + lane);
     }
     __syncwarp();
-    for (int q = lane; q < NP; q += 32) {  // B = L T, lower (L from Ai)
+    // B = L T with L = U^-T, by forward substitution U' B = T (row i:
+    // B[i][.] = (T[i][.] - sum_{k<i} U[k][i] B[k][.]) / U[i][i]), right-
+    // looking so that each row costs two dependent FP64 operations; B is
+    // lower triangular like T
+    for (int q = lane; q < NP; q += 32) {
       int i, j;
       rc_of(q, i, j);
-      double s = 0.0;
-      for (int k = j; k <= i; ++k) s += Ai[i][k] * T[k][j];
-      B[i][j] = s;
+      B[i][j] = T[i][j];
+    }
+    __syncwarp();
+    for (int i = 0; i < P; ++i) {
+      if (lane <= i) B[i][lane] *= rd[i];
+      __syncwarp();
+      // rows r > i, columns j <= i: (P - 1 - i)(i + 1) <= 16 entries
+      const int nr = P - 1 - i;
+      if (lane < nr * (i + 1)) {
+        const int r = i + 1 + lane / (i + 1), j = lane - (lane / (i + 1)) * (i + 1);
+        B[r][j] -= A[i][r] * B[i][j];
+      }
+      __syncwarp();
     }
     __syncwarp();
     bool fin = true;

@@ -243,11 +243,12 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
           aq[2 * h] = __uint_as_float(__float_as_uint(a.x) ^ ((yw4 >> (2 * h)) << 31));
           aq[2 * h + 1] = __uint_as_float(__float_as_uint(a.y) ^ ((yw4 >> (2 * h + 1)) << 31));
         }
+        // (a subject beyond kATail gets a meaningless inversion here; the
+        // rejection sampler below replaces it)
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-          const float2 t = tn_lower_inv2(
-              make_float2(fminf(aq[2 * h], kATail), fminf(aq[2 * h + 1], kATail)),
-              pick4(r, 2 * h), pick4(r, 2 * h + 1));
+          const float2 t = tn_lower_inv2(make_float2(aq[2 * h], aq[2 * h + 1]),
+                                         pick4(r, 2 * h), pick4(r, 2 * h + 1));
           const uint32_t y0 = (yw4 >> (2 * h)) << 31, y1 = (yw4 >> (2 * h + 1)) << 31;
           zh[h] = add2(m0h[h],
                        make_float2(__uint_as_float(__float_as_uint(t.x) ^ y0 ^ 0x80000000u),
@@ -326,9 +327,9 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           const int q0 = 2 * h, q1 = q0 + 1;
-          const float2 t = tn_lower_inv2(
-              make_float2(fminf(aq[q0], kATail), fminf(aq[q1], kATail)), pick4(r, q0),
-              pick4(r, q1));
+          // (beyond kATail the inversion is replaced by the rejection draw)
+          const float2 t = tn_lower_inv2(make_float2(aq[q0], aq[q1]), pick4(r, q0),
+                                         pick4(r, q1));
           const float2 rr = mul2(t, make_float2(sdq[q0], sdq[q1]));
           rq[q0] = __uint_as_float(__float_as_uint(rr.x) ^ ((yw4 >> q0) << 31) ^ 0x80000000u);
           rq[q1] = __uint_as_float(__float_as_uint(rr.y) ^ ((yw4 >> q1) << 31) ^ 0x80000000u);

@@ -188,8 +188,8 @@ __global__ void __launch_bounds__(kPredThreads, pred_min_blocks<P, S>())
         // voxels k, k + 1 of one pair row, then an odd last voxel alone from
         // the .x halves
         int k = k0;
-#pragma unroll 2
-        for (; k + 1 < k1; k += 2) {
+#pragma unroll 1
+        for (; k + 1 < k1; k += 2) {  // (measured: unroll 1 < 4 < 2 in time)
           float2 bp[2 * R2];
 #pragma unroll
           for (int u = 0; u < R2; ++u) {

@@ -19,21 +19,24 @@
 // memory, so one Philox call serves four consecutive subjects of one lane.
 #pragma once
 
+#include <type_traits>
+
 #include "bsg_wishart.cuh"
 
 namespace bsg {
 
 // Resident 256-thread blocks per SM asked of ptxas: three (80 registers) up
-// to P = 6, two (128 registers) above, measured fastest on the brain-sized
-// study (P = 5) and the 1.5M-voxel study (P = 6, 2.16 -> 2.11 ms per sweep
-// against two blocks); BSG_FUSED_MIN_BLOCKS overrides it for tuning builds.
+// to P = 5, two (128 registers) above, measured fastest on the brain-sized
+// study (P = 5) and the 1.5M-voxel study (P = 6: 2.00 against 2.02 ms per
+// sweep with three blocks, which spill); BSG_FUSED_MIN_BLOCKS overrides it
+// for tuning builds.
 template <int P, bool MIX = false>
 constexpr int fused_min_blocks() {
 #ifdef BSG_FUSED_MIN_BLOCKS
   return BSG_FUSED_MIN_BLOCKS;
 #else
   // the t/logit kernel also keeps the voxel's X' Phi X in registers
-  return MIX ? (P <= 5 ? 2 : 1) : (P <= 6 ? 3 : 2);
+  return MIX ? (P <= 5 ? 2 : 1) : (P <= 5 ? 3 : 2);
 #endif
 }
 
@@ -216,18 +219,22 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
             acc[p] = fmaf(x[p], zr, acc[p]);
         }
       };
-      // The probit group of four on subject pairs (PAIRX): x'beta, the
-      // inversion and X'(Z - bwm) each as two f32x2 pairs, subjects
-      // (ii0, ii0 + 1) and (ii0 + 2, ii0 + 3).  Per subject the same
-      // arithmetic as `subject`; the even and odd subjects' X'Z sums are
-      // kept apart until the end of the voxel.
-      auto group4p = [&](int ii0, uint32_t yw4, uint4 r, uint32_t i) {
-        const int m = ii0 >> 1;  // even: rows m, m + 1 share one pad group
+      // The probit groups on subject pairs (PAIRX): G groups of four subjects
+      // (G Philox calls), x'beta, the inversion and X'(Z - bwm) each as 2G
+      // f32x2 pairs of subjects (ii0 + 2h, ii0 + 2h + 1); one tail vote for
+      // all 4G.  Per subject the same arithmetic as `subject`; the even and
+      // odd subjects' X'Z sums are kept apart until the end of the voxel.
+      // G = 2 gives the scheduler four independent pair chains (measured
+      // 1.6 % faster per sweep than G = 1, with identical results).
+      auto groupp = [&](auto gsz, int ii0, uint32_t ywg, const uint4 *rs, uint32_t i) {
+        constexpr int G = decltype(gsz)::value;
+        constexpr int H = 2 * G;
+        const int m = ii0 >> 1;  // a multiple of H: rows m..m+H-1 share one pad group
         const float *xr0 = &Xs[m * RW + (m >> 4) * 4];
-        float2 m0h[2], zh[2];
-        float aq[4];
+        float2 m0h[H], zh[H];
+        float aq[2 * H];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
+        for (int h = 0; h < H; ++h) {
           const float *xr = xr0 + h * RW;
           float2 s = make_float2(0.f, 0.f);
 #pragma unroll
@@ -240,26 +247,28 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
             s = fma2(*reinterpret_cast<const float2 *>(xr + 2 * (P - 1)), bb[P - 1], s);
           m0h[h] = s;
           const float2 a = add2(s, make_float2(bwm, bwm));
-          aq[2 * h] = __uint_as_float(__float_as_uint(a.x) ^ ((yw4 >> (2 * h)) << 31));
-          aq[2 * h + 1] = __uint_as_float(__float_as_uint(a.y) ^ ((yw4 >> (2 * h + 1)) << 31));
+          aq[2 * h] = __uint_as_float(__float_as_uint(a.x) ^ ((ywg >> (2 * h)) << 31));
+          aq[2 * h + 1] = __uint_as_float(__float_as_uint(a.y) ^ ((ywg >> (2 * h + 1)) << 31));
         }
         // (a subject beyond kATail gets a meaningless inversion here; the
         // rejection sampler below replaces it)
+        float amax = aq[0];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
+        for (int h = 0; h < H; ++h) {
+          const uint4 rr = rs[h >> 1];
           const float2 t = tn_lower_inv2(make_float2(aq[2 * h], aq[2 * h + 1]),
-                                         pick4(r, 2 * h), pick4(r, 2 * h + 1));
-          const uint32_t y0 = (yw4 >> (2 * h)) << 31, y1 = (yw4 >> (2 * h + 1)) << 31;
+                                         pick4(rr, (2 * h) & 3), pick4(rr, (2 * h + 1) & 3));
+          const uint32_t y0 = (ywg >> (2 * h)) << 31, y1 = (ywg >> (2 * h + 1)) << 31;
           zh[h] = add2(m0h[h],
                        make_float2(__uint_as_float(__float_as_uint(t.x) ^ y0 ^ 0x80000000u),
                                    __uint_as_float(__float_as_uint(t.y) ^ y1 ^ 0x80000000u)));
+          amax = fmaxf(amax, fmaxf(aq[2 * h], aq[2 * h + 1]));
         }
-        const bool far = fmaxf(fmaxf(aq[0], aq[1]), fmaxf(aq[2], aq[3])) > kATail;
-        if (__any_sync(__activemask(), far)) {
+        if (__any_sync(__activemask(), amax > kATail)) {
 #pragma unroll
-          for (int q = 0; q < 4; ++q)
+          for (int q = 0; q < 2 * H; ++q)
             if (aq[q] > kATail) {
-              const uint32_t ym = (yw4 >> q) << 31;
+              const uint32_t ym = (ywg >> q) << 31;
               const float t = tn_lower_tail(aq[q], i + q, (uint32_t)v, sweep,
                                             cid | kTagZTail, ch.key0, ch.key1, &ok);
               const float m0 = (q & 1) ? m0h[q >> 1].y : m0h[q >> 1].x;
@@ -271,7 +280,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
             }
         }
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
+        for (int h = 0; h < H; ++h) {
           const float *xr = xr0 + h * RW;
 #pragma unroll
           for (int p = 0; p + 1 < P; p += 2) {
@@ -415,6 +424,18 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
 #pragma unroll
             for (int q = 0; q < 4; ++q) phc[q] = phb[(size_t)(i00 + q) * nc];
           }
+          if constexpr (PAIRX) {
+#pragma unroll 1
+            for (int b = 0; b < 32; b += 8) {
+              const uint32_t i = i00 + (uint32_t)b;
+              const uint4 rs[2] = {
+                  philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key),
+                  philox(make_uint4((i >> 2) + 1, (uint32_t)v, sweep, cid | kTagZ), key)};
+              groupp(std::integral_constant<int, 2>{}, (wl << 5) + b, yw, rs, i);
+              yw >>= 8;
+            }
+            continue;
+          }
 #pragma unroll 1
           for (int b = 0; b < 32; b += 4) {
             const uint32_t i = i00 + (uint32_t)b;
@@ -424,10 +445,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
             }
             uint4 r = make_uint4(0, 0, 0, 0);
             if (!SUPP) r = philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key);
-            if constexpr (PAIRX) {
-              group4p((wl << 5) + b, yw, r, i);
-              yw >>= 4;
-            } else if constexpr (MIX) {
+            if constexpr (MIX) {
               group4_mix(xo + b, yw, r, i, gpair(i), gpair(i + 2), phc);
               yw >>= 4;
             } else {
@@ -452,7 +470,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
             if (!SUPP) r = philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key);
             if constexpr (PAIRX) {
               if (b + 4 <= nbits) {  // a whole group of the last word
-                group4p((wl << 5) + b, yw, r, i);
+                groupp(std::integral_constant<int, 1>{}, (wl << 5) + b, yw, &r, i);
                 yw >>= 4;
                 continue;
               }

@@ -16,7 +16,9 @@
 //
 // Work mapping: LPV lanes per voxel; each lane takes whole 32-subject
 // outcome words (w = k, k+LPV, ...) of a subject chunk staged in shared
-// memory, so one Philox call serves four consecutive subjects of one lane.
+// memory, so one Philox call serves four consecutive subjects of one lane
+// (the probit kernel takes two calls, eight subjects, per step, and does
+// its FP32 arithmetic on pairs of subjects with the f32x2 instructions).
 #pragma once
 
 #include <type_traits>

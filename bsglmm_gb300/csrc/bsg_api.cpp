@@ -1012,7 +1012,6 @@ bsg_status bsg_get_beta(bsg_ctx *ctx, int32_t chain, float *out) {
   const Chain &c = ctx->ch[chain];
   const Dataset &d = ctx->ds[c.dataset];
   CK(cudaSetDevice(ctx->device));
-  CK(cudaStreamSynchronize(ctx->stream));
   CK(d2h(ctx, out, c.dev.beta, sizeof(float) * (size_t)d.P * d.Vp));
   return BSG_OK;
 }
@@ -1031,7 +1030,6 @@ bsg_status bsg_set_beta(bsg_ctx *ctx, int32_t chain, const float *in) {
     for (int s = 0; s < d.Vp; ++s)
       if (!inmask[s]) b[(size_t)p * d.Vp + s] = 0.f;
   CK(cudaSetDevice(ctx->device));
-  CK(cudaStreamSynchronize(ctx->stream));
   CK(h2d(ctx, c.dev.beta, b.data(), sizeof(float) * b.size()));
   return BSG_OK;
 }
@@ -1041,7 +1039,6 @@ bsg_status bsg_get_omega(bsg_ctx *ctx, int32_t chain, double *out) {
   const Chain &c = ctx->ch[chain];
   const int P = ctx->ds[c.dataset].P;
   CK(cudaSetDevice(ctx->device));
-  CK(cudaStreamSynchronize(ctx->stream));
   CK(d2h(ctx, out, c.dev.omega_d, sizeof(double) * P * P));
   return BSG_OK;
 }
@@ -1052,7 +1049,6 @@ bsg_status bsg_set_omega(bsg_ctx *ctx, int32_t chain, const double *in) {
   const int P = ctx->ds[c.dataset].P;
   std::vector<float> f(in, in + P * P);
   CK(cudaSetDevice(ctx->device));
-  CK(cudaStreamSynchronize(ctx->stream));
   CK(h2d(ctx, c.dev.omega_d, in, sizeof(double) * P * P));
   CK(h2d(ctx, c.dev.omega_f, f.data(), sizeof(float) * P * P));
   return BSG_OK;
@@ -1107,7 +1103,6 @@ bsg_status bsg_get_colmeans(bsg_ctx *ctx, int32_t chain, float *out) {
   if (!valid_chain(ctx, chain) || !out) return BSG_ERR_INVALID;
   const Chain &c = ctx->ch[chain];
   CK(cudaSetDevice(ctx->device));
-  CK(cudaStreamSynchronize(ctx->stream));
   CK(d2h(ctx, out, c.dev.colmean, sizeof(float) * ctx->ds[c.dataset].P));
   return BSG_OK;
 }
@@ -1116,7 +1111,6 @@ bsg_status bsg_get_sweep(bsg_ctx *ctx, int32_t chain, int64_t *sweep, int64_t *n
   if (!valid_chain(ctx, chain)) return BSG_ERR_INVALID;
   ChainCounters h{};
   CK(cudaSetDevice(ctx->device));
-  CK(cudaStreamSynchronize(ctx->stream));
   CK(d2h(ctx, &h, counters_of(ctx->ch[chain]), sizeof(h)));
   if (sweep) *sweep = h.sweep[1];
   if (nkept) *nkept = h.nkept;
@@ -1546,7 +1540,6 @@ bsg_status bsg_predict(bsg_ctx *ctx, int32_t chain, double *mpredict) {
   CK(launch_predict_finish(ctx->d_ds, ctx->d_ch, nullptr,
                            (d.N + kPredWarps - 1) / kPredWarps, chain, kPredNow,
                            ctx->stream, false));
-  CK(cudaStreamSynchronize(ctx->stream));
   CK(d2h(ctx, mpredict, c.dev.mpred, sizeof(double) * (size_t)d.N * d.S));
   return BSG_OK;
 }

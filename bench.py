@@ -53,6 +53,11 @@ CPU_REFERENCE_S = 90.0  # seconds of CPU work in a whole reference-arm run
 # 43.89 + 0.09 MB).  ncu cannot run inside a timed bench, so the captured
 # figure is carried here and reported only for that workload.
 NCU_TRAFFIC_PER_LAUNCH = 43.935e6
+# Thread instructions per subject-voxel update of the same capture's colour
+# launches (smsp__inst_executed x 32 / updates, the mean of 60.1 and 60.6):
+# the issue-slot roofline below divides the instruction rate this implies
+# by the SMs' issue peak (4 warp instructions per clock per SM).
+NCU_INST_PER_UPDATE = 60.35
 
 
 def fused_flops_per_update(P: int) -> int:
@@ -134,6 +139,28 @@ class Clocks:
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": mx, "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def issue_roofline(device: int, updates_per_s: float):
+    """The binding resource of the colour kernel is issue slots: thread
+    instructions per second (ncu's instructions per update x the live update
+    rate of a colour launch) against 4 warp instructions per clock per SM at
+    the maximum SM clock."""
+    try:
+        import torch
+        props = torch.cuda.get_device_properties(device)
+        sms = props.multi_processor_count
+        mhz = float(subprocess.run(
+            ["nvidia-smi", "-i", str(device), "--query-gpu=clocks.max.sm",
+             "--format=csv,noheader,nounits"], capture_output=True, text=True,
+            timeout=20).stdout.strip().splitlines()[0])
+    except Exception:
+        return None
+    achieved = NCU_INST_PER_UPDATE * updates_per_s / 1e12
+    peak = 4 * 32 * sms * mhz * 1e6 / 1e12
+    return {"achieved": achieved, "peak": peak, "unit": "Tinst/s (thread instructions)",
+            "frac": achieved / peak, "inst_per_update": NCU_INST_PER_UPDATE,
+            "inst_source": "ncu capture of the same workload"}
 
 
 def measured_peaks():
@@ -353,6 +380,7 @@ def run_ours(args, rank, world, local):
             "hbm_bytes_per_sweep": sweep_bytes(N, V, P, S),
             "hbm_achieved_gbs": sweep_bytes(N, V, P, S) / (ms_per_step * 1e-3) / 1e9,
             "hbm_peak_gbs": peaks.get("hbm_gbs"),
+            "issue": issue_roofline(local, N * V / 2 / (fused_avg_ms * 1e-3)),
         },
         "cpu_baseline": cpu,
         "clocks": clocks,

@@ -436,33 +436,33 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
               groupp(std::integral_constant<int, 2>{}, (wl << 5) + b, yw, rs, i);
               yw >>= 8;
             }
-            continue;
-          }
+          } else {
 #pragma unroll 1
-          for (int b = 0; b < 32; b += 4) {
-            const uint32_t i = i00 + (uint32_t)b;
-            if (MIX && b + 4 < 32) {
+            for (int b = 0; b < 32; b += 4) {
+              const uint32_t i = i00 + (uint32_t)b;
+              if (MIX && b + 4 < 32) {
 #pragma unroll
-              for (int q = 0; q < 4; ++q) phx[q] = phb[(size_t)(i + 4 + q) * nc];
-            }
-            uint4 r = make_uint4(0, 0, 0, 0);
-            if (!SUPP) r = philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key);
-            if constexpr (MIX) {
-              group4_mix(xo + b, yw, r, i, gpair(i), gpair(i + 2), phc);
-              yw >>= 4;
-            } else {
-              const uint4 g0 = gpair(i), g1 = gpair(i + 2);
-#pragma unroll
-              for (int q = 0; q < 4; ++q) {
-                const uint4 gq = q < 2 ? g0 : g1;
-                subject(xo + b + q, yw << 31, variate(r, q, i + q), i + q,
-                        (q & 1) ? gq.z : gq.x, (q & 1) ? gq.w : gq.y, phc[q]);
-                yw >>= 1;
+                for (int q = 0; q < 4; ++q) phx[q] = phb[(size_t)(i + 4 + q) * nc];
               }
-            }
-            if (MIX) {
+              uint4 r = make_uint4(0, 0, 0, 0);
+              if (!SUPP) r = philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key);
+              if constexpr (MIX) {
+                group4_mix(xo + b, yw, r, i, gpair(i), gpair(i + 2), phc);
+                yw >>= 4;
+              } else {
+                const uint4 g0 = gpair(i), g1 = gpair(i + 2);
 #pragma unroll
-              for (int q = 0; q < 4; ++q) phc[q] = phx[q];
+                for (int q = 0; q < 4; ++q) {
+                  const uint4 gq = q < 2 ? g0 : g1;
+                  subject(xo + b + q, yw << 31, variate(r, q, i + q), i + q,
+                          (q & 1) ? gq.z : gq.x, (q & 1) ? gq.w : gq.y, phc[q]);
+                  yw >>= 1;
+                }
+              }
+              if (MIX) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) phc[q] = phx[q];
+              }
             }
           }
         } else {

@@ -16,7 +16,7 @@ constexpr int kPostVals = kMaxPairs + kMaxP;        // pairs + column sums
 constexpr int kP0Vals = kMaxP + 1;
 constexpr int kFusedVals = kPostVals + 1;
 constexpr int kWmOff = kPostVals;                    // beta_WM term's slot
-constexpr int kChunk = 512;                         // subjects staged per pass
+constexpr int kChunk = 1024;                        // subjects staged per pass
 constexpr int kChunkPad = kChunk + kChunk / 32;     // one pad word per 32
 constexpr float kATail = 5.0f;  // inversion below, rejection above
 constexpr int kTailMax = 16;    // rejection attempts per latent draw

@@ -1,5 +1,5 @@
 """Edge shapes of the colour kernels against the FP64 oracle chain on the
-same counters: more subjects than one shared-memory chunk (512) with a
+same counters: more subjects than one shared-memory chunk (1024) with a
 partial last outcome word, a single subject, single-voxel masks (one colour
 empty), and several P at once in one context."""
 from __future__ import annotations
@@ -44,10 +44,11 @@ def _compare(oracle_mod, mask, covar, data, S, seed, sweeps=2):
         s.sync()
 
 
-@pytest.mark.parametrize("N", [600, 1025])
+@pytest.mark.parametrize("N", [600, 1025, 2100])
 def test_subjects_across_chunks_and_partial_word(oracle_mod, N):
-    """600 = 512 + 88 and 1025 = 2 x 512 + 1: two or three shared-memory
-    chunks, the last outcome word partial (24 and 1 subjects)."""
+    """600 (one chunk, the last word 24 subjects), 1025 = 1024 + 1 and
+    2100 = 2 x 1024 + 52: one to three shared-memory chunks, partial last
+    outcome words."""
     mask, covar, data, S = _study(3, (6, 6, 5), N, 3)
     _compare(oracle_mod, mask, covar, data, S, seed=0xC0FFEE)
 

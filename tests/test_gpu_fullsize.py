@@ -119,7 +119,7 @@ def test_largest_study_batched_chain_equals_lone_chain():
 
 
 def test_precision_form_graph_segment_and_posterior_sums():
-    """The N = 2000, P = 8 study on the brain mask (four 512-subject chunks,
+    """The N = 2000, P = 8 study on the brain mask (two 1024-subject chunks,
     the two-block P = 8 kernel): a 4-sweep graph segment equals 4 single
     sweeps, and the posterior sums equal the recorded maps of the kept
     sweeps 1-3."""

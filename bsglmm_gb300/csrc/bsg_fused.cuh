@@ -184,7 +184,10 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
             gm = gamma_mt_more(ch.mix_d, ch.mix_c, isub, (uint32_t)v, sweep,
                                cid | kTagPhiMore, ch.key0, ch.key1, &ok);
           }
-          const float phn = 2.f * gm / fmaf(r, r, ch.t_df);
+          // the new weight 2 g / (r^2 + nu) with a MUFU reciprocal (r^2 + nu
+          // >= 3; a few ulp, where the IEEE division's check and slow path
+          // cost 4-6 % of the sweep)
+          const float phn = __fmul_rn(2.f * gm, rcp_approx(fmaf(r, r, ch.t_df)));
           *pp = phn;
           const float wz = phn * zr;
           float px[P];
@@ -382,7 +385,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
         for (int q = 0; q < 4; ++q) {
           float x[P];
           row(col0 + q, x);
-          const float phn = 2.f * gq[q] / fmaf(rq[q], rq[q], ch.t_df);
+          const float phn = __fmul_rn(2.f * gq[q], rcp_approx(fmaf(rq[q], rq[q], ch.t_df)));
           ch.phi[colour][(size_t)(i + q) * nc + j] = phn;
           const float wz = phn * (m0q[q] + rq[q]);
           float px[P];

@@ -138,3 +138,29 @@ def test_reset_accumulators_is_ordered_with_the_sweeps():
             assert np.allclose(mean, tr.mean(0), rtol=1e-12, atol=1e-12)
             assert np.allclose(var, tr.var(0, ddof=1), rtol=1e-6, atol=1e-9)
             assert var.min() > -1e-9
+
+
+def test_page_locked_host_buffers():
+    """The accessors take page-locked host buffers as well as pageable ones:
+    an upload from a page-locked buffer that the caller overwrites right
+    after the call, and a download into one, read the values of the call."""
+    torch = pytest.importorskip("torch")
+    import bsglmm_gb300 as bsg
+    from bsglmm_gb300.sampler import _ptr
+    mask, covar, data, S = _study(41, (8, 7, 6), 40, 3)
+    with bsg.Sampler() as s:
+        ds = s.add_dataset(mask, covar, data, S)
+        ch = s.add_chain(ds, seed=3)
+        P = 3
+        pin_in = torch.empty(P * P, dtype=torch.float64, pin_memory=True).numpy()
+        pin_out = torch.empty(P * P, dtype=torch.float64, pin_memory=True).numpy()
+        target = np.array([[2.0, 0.3, 0.1], [0.3, 1.5, 0.2], [0.1, 0.2, 1.2]])
+        pin_in[:] = target.ravel()
+        assert s._L.bsg_set_omega(s._h, ch, _ptr(pin_in)) == 0
+        pin_in[:] = -7.0  # the caller reuses its buffer at once
+        assert s._L.bsg_get_omega(s._h, ch, _ptr(pin_out)) == 0
+        assert np.array_equal(pin_out.reshape(P, P), target)
+        s.run(2, sync=False)
+        assert s._L.bsg_get_omega(s._h, ch, _ptr(pin_out)) == 0
+        assert np.array_equal(pin_out.reshape(P, P), s.omega(ch))
+        assert not np.array_equal(pin_out.reshape(P, P), target)

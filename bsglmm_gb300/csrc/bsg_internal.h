@@ -111,7 +111,7 @@ struct ChainDev {
   // DIC / Qhat predictive pass (null until first used)
   int32_t pred_tiles;      // voxel tiles of the predictive pass
   int32_t pred_tile;       // voxels per tile (a multiple of kPredThreads)
-  double *pred_part;       // [tiles][N][max(S,1)] per-tile subject sums
+  double *pred_part;       // [N][max(S,1)][tiles] per-tile subject sums
   double *pred_subj;       // [N] each subject's term of the ED / DE sum
   double *mpred;           // [N][S] Mpredict of the last pass
   double *qhat;            // [N][S] Qhat, log scale (mcmc.cpp:223-225)

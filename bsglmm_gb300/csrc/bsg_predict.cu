@@ -20,8 +20,8 @@
 //
 // predict_finish_kernel: one warp per subject sums the tile partials in a
 // fixed order (lane l takes tiles l, l + 32, ...; xor-shuffle tree), so the
-// result does not depend on scheduling; lane 0 updates Qhat
-// (covarGPU.cu:1937-1953) and stores the subject's own-group term; the last
+// result does not depend on scheduling; lanes 0..S-1 update Qhat
+// (covarGPU.cu:1937-1953), lane 0 stores the subject's own-group term; the last
 // block to arrive adds them, in subject order, to the ED sum.
 //
 // Log probabilities: PhiAS(-x) = 1 - PhiAS(x) holds exactly for the A&S
@@ -247,11 +247,13 @@ __global__ void __launch_bounds__(kPredThreads, pred_min_blocks<P, S>())
     }
   }
   if (i < N) {
+    // [subject][column][tile]: the finishing warp of a subject then reads
+    // its tiles from consecutive addresses
     const int G = de ? 1 : S;
-    double *out = ch.pred_part + ((size_t)tile * N + i) * G;
+    double *out = ch.pred_part + (size_t)i * G * ch.pred_tiles + tile;
 #pragma unroll
     for (int g = 0; g < S; ++g)
-      if (g < G) out[g] = acc[g];
+      if (g < G) out[(size_t)g * ch.pred_tiles] = acc[g];
   }
 }
 
@@ -279,9 +281,11 @@ __global__ void __launch_bounds__(kPredWarps * 32)
     for (int g = 0; g < kMaxP; ++g) {
       double s = 0.0;
       if (g < G) {
-        // four loads in flight per lane; the sum keeps tile order
+        // consecutive tiles across the lanes, four loads in flight per lane;
+        // the sum keeps tile order
+        const double *src = ch.pred_part + ((size_t)i * G + g) * T;
 #pragma unroll 4
-        for (int t = lane; t < T; t += 32) s += ch.pred_part[((size_t)t * N + i) * G + g];
+        for (int t = lane; t < T; t += 32) s += __ldcg(src + t);
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);

@@ -16,7 +16,14 @@
 // library holds it (1.4 MB) until the process exits, and every call on a
 // device shares it.  Calls that may overlap on the GPU (different streams,
 // no ordering between them) race on it and must be serialised by the
-// caller.
+// caller.  The kernel keeps its small FP64 matrices in shared memory, so a
+// launch needs no per-thread local-memory frame beyond a few spilled words.
+//
+// The first call in a process (and the first after a device reset) looks
+// the array's device address up; because this library's kernels are loaded
+// lazily, that first call also loads this file's module onto the device.
+// Callers should therefore make one call at start-up, before any stream
+// capture and before their own memory budget is fixed.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -60,8 +67,9 @@ __device__ bool na_chol(double *A, int n) {
   return true;
 }
 
-__device__ void na_inverse(const double *G, int n, double *out) {
-  double col[kMaxP];
+// Inverse of G G' from the lower factor G, column by column (the scheme of
+// cholesky.cpp:55-86); col is a work column of n doubles.
+__device__ void na_inverse(const double *G, int n, double *out, double *col) {
   for (int k = 0; k < n; ++k) {
     for (int i = 0; i < n; ++i) col[i] = (i == k) ? 1.0 : 0.0;
     for (int i = 0; i < n; ++i) {
@@ -101,18 +109,22 @@ __device__ double na_gamma(double a, uint32_t slot, const NaArgs &g, int *err) {
 }
 
 // Bartlett draw after chol -> invert -> chol of S + I (the reference's
-// covar.cpp:286-295 with cholesky.cpp:245-286), FP64, one thread.
-__device__ void na_wishart(const NaArgs &g, const double *tot) {
+// covar.cpp:286-295 with cholesky.cpp:245-286), FP64, one thread.  The
+// sampler's own draw (the last colour-1 block of bsg_run) reaches the same
+// factor chol((S + I)^-1) by a reverse Cholesky instead: the factor is
+// unique, so the two differ only by rounding.  wk holds the four P x P
+// work matrices (shared memory of the calling block).
+__device__ void na_wishart(const NaArgs &g, const double *tot, double *wk) {
   const int P = g.P;
-  double A[kMaxP * kMaxP], Ai[kMaxP * kMaxP], T[kMaxP * kMaxP];
-  double B[kMaxP * kMaxP];
+  double *A = wk, *Ai = wk + kMaxP * kMaxP, *T = wk + 2 * kMaxP * kMaxP;
+  double *B = wk + 3 * kMaxP * kMaxP;
   int err = 0;
   for (int r = 0; r < P; ++r)
     for (int c = 0; c <= r; ++c)
       A[c + r * P] = A[r + c * P] = tot[tri(r, c)] + (r == c ? 1.0 : 0.0);
   bool ok = na_chol(A, P);
   if (ok) {
-    na_inverse(A, P, Ai);
+    na_inverse(A, P, Ai, B);  // B is free until the Bartlett product
     ok = na_chol(Ai, P);
   }
   if (ok) {
@@ -160,14 +172,20 @@ __device__ void na_wishart(const NaArgs &g, const double *tot) {
   if (g.status) *g.status = err;
 }
 
-// The Omega half of post_sweep_kernel with its block partials and arrival
-// counter in the caller-independent scratch array.  Voxel positions,
-// per-voxel products and the block/partial order are those of the
-// post-sweep pass, so the result equals the sampler's.
+// S = sum over in-mask voxels and their forward neighbours (+x, +y, +z) of
+// the pair products, with the reference's indicator (the neighbour's row
+// coefficient is nonzero, covar.cpp:235-253): the same edges and
+// indicator as the sampler, which counts each edge from its colour-1 end
+// over all six neighbours.  Here each thread sums its voxels' FP32 products
+// in FP64, the block partials go to the scratch array, and the last block
+// to arrive sums them in block order and draws Omega.  The sampler sums in
+// FP32 warp trees first, so the two Omegas agree to rounding (about 1e-6
+// relative), not bit for bit.
 __global__ void __launch_bounds__(kPostThreads)
     omega_noalloc_kernel(NaArgs g, unsigned long long *scratch) {
   __shared__ double red[kPostThreads / 32][kMaxPairs];
   __shared__ double tot[kMaxPairs];
+  __shared__ double wk[4 * kMaxP * kMaxP];
   __shared__ int is_last;
   const int P = g.P, npairs = P * (P + 1) / 2;
   double accp[kMaxPairs];
@@ -241,14 +259,28 @@ __global__ void __launch_bounds__(kPostThreads)
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    na_wishart(g, tot);
+    na_wishart(g, tot, wk);
     scratch[0] = 0ull;  // leave the counter cleared for the next call
   }
 }
 
-// Device address of the scratch array, looked up once per device.
+// Device address of the scratch array, looked up once per device and
+// context.  The runtime's host-side symbol is only a stand-in: the address
+// on the device comes from cudaGetSymbolAddress with the device current.
+// A cudaDeviceReset destroys the context and the module with it, so the
+// cache is keyed on the current driver context (cuCtxGetCurrent, reached
+// through the runtime's driver entry point, so the library does not link
+// libcuda itself) and looked up again when that changes.
+typedef int (*CtxGetCurrentFn)(void **);
+
+struct NaSlot {
+  void *ctx = nullptr;
+  unsigned long long *ptr = nullptr;
+};
 std::mutex g_na_mutex;
-unsigned long long *g_na_ptr[256] = {nullptr};
+NaSlot g_na_slot[256];
+CtxGetCurrentFn g_ctx_get = nullptr;
+bool g_ctx_tried = false;
 
 cudaError_t scratch_for_current_device(unsigned long long **out) {
   int dev = 0;
@@ -256,13 +288,29 @@ cudaError_t scratch_for_current_device(unsigned long long **out) {
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lk(g_na_mutex);
-  if (!g_na_ptr[dev]) {
+  if (!g_ctx_tried) {
+    g_ctx_tried = true;
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuCtxGetCurrent", &fn, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_ctx_get = reinterpret_cast<CtxGetCurrentFn>(fn);
+  }
+  // (before the device's first runtime call no context is current yet:
+  // the lookup below creates it, and the next call caches it)
+  void *ctx = nullptr;
+  if (g_ctx_get && g_ctx_get(&ctx) != 0) ctx = nullptr;
+  NaSlot &slot = g_na_slot[dev];
+  // without the driver entry point every call looks the address up again
+  if (!slot.ptr || !ctx || slot.ctx != ctx) {
     void *p = nullptr;
     e = cudaGetSymbolAddress(&p, g_omega_scratch);
     if (e != cudaSuccess) return e;
-    g_na_ptr[dev] = static_cast<unsigned long long *>(p);
+    slot.ptr = static_cast<unsigned long long *>(p);
+    slot.ctx = ctx;
   }
-  *out = g_na_ptr[dev];
+  *out = slot.ptr;
   return cudaSuccess;
 }
 

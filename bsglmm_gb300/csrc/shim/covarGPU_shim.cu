@@ -7,7 +7,7 @@
 // libbsglmm_gb300.so, reading the study from the reference's own globals
 // (NSUBS, NROW, ..., hostIdx, covar).  Link it with the reference's
 // main.cu, mcmc.cpp, read_data.cpp, randgen.cpp, cholesky.cpp and covar.cpp
-// instead of covarGPU.cu (see INTEGRATION.md).
+// instead of covarGPU.cu.
 //
 // Mapping onto the fused sampler:
 //   updateZGPU            records the outcome array and beta_WM: the latent

@@ -239,14 +239,20 @@ bsg_status bsg_sweep_supplied(bsg_ctx *ctx, int32_t chain,
  * bsg_get_lattice returns them), idxsc the padded -> compact dilated map,
  * omega [P][P] (output, FP64), status (optional, 1 int: 0 or error bits).
  * chi2 [P] and wnorm [P(P-1)/2] supply the Bartlett variates; pass both
- * NULL to draw them from (seed, chain_id, sweep) as bsg_run does.
+ * NULL to draw them from (seed, chain_id, sweep) as bsg_run does.  Omega
+ * equals the sampler's draw from the same coefficients and variates to
+ * rounding (the tests hold it to 1e-5 relative): the pair sums are formed
+ * in a different order and the factor chol((S + I)^-1) by chol -> invert ->
+ * chol instead of the sampler's reverse Cholesky.
  *
  * Its reduction scratch is a fixed 1.4 MB array inside the library, held
  * by every GPU that loads it until exit and shared by every call on that
  * device: calls that can overlap on the GPU race and must be serialised by
- * the caller.  The first call on each device looks the array up
- * (cudaGetSymbolAddress); make that call before any stream capture.
- * Asynchronous on `stream`.  V > BSG_NOALLOC_MAX_VOXELS returns
+ * the caller.  The first call on each device (and the first after a
+ * cudaDeviceReset) looks the array up (cudaGetSymbolAddress) and, as the
+ * library's kernels load lazily, loads this kernel's module: make that
+ * first call at start-up, before any stream capture.  Later calls reserve
+ * nothing.  Asynchronous on `stream`.  V > BSG_NOALLOC_MAX_VOXELS returns
  * BSG_ERR_UNSUPPORTED. */
 bsg_status bsg_omega_update_noalloc(const float *spatcoef, const int32_t *vox,
                                     const int32_t *idxsc, int32_t nrow,

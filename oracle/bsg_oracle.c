@@ -10,6 +10,7 @@
 
 #include <float.h>
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -723,6 +724,93 @@ double orc_mix_gamma(double alpha, uint32_t i, uint32_t v, uint32_t sweep,
   return mix_gamma(&cfg, d, 1.0 / sqrt(9.0 * d), i, v, sweep, &err);
 }
 
+/* Host threads of orc_chain_run (voxels of one colour are independent given
+ * the other colour, so a colour's voxel list is split into contiguous
+ * ranges; results do not depend on the thread count except for the order
+ * of the beta_WM sum). */
+static int g_orc_threads = 1;
+void orc_set_threads(int n) { g_orc_threads = n < 1 ? 1 : (n > 256 ? 256 : n); }
+
+typedef struct {
+  const orc_problem *pb;
+  const orc_chain_cfg *cfg;
+  double *spatcoef, *phi;
+  const double *omega, *xsum;
+  double bw, md, mc, nu;
+  int mix, c;
+  uint32_t sw;
+  int j0, j1;
+  double wmr; /* out: this range's term of the beta_WM conditional mean */
+  int err;    /* out */
+} chain_range;
+
+/* Z_v then beta_v for the voxels j0..j1-1 of colour c (covar.cpp:302-325
+ * and 121-187 on the sampler's counters). */
+static void chain_colour_range(chain_range *r) {
+  const orc_problem *pb = r->pb;
+  const orc_chain_cfg *cfg = r->cfg;
+  int N = pb->N, P = pb->P, V = pb->V, Vp = pb->Vp, c = r->c, err = 0;
+  uint32_t k0 = cfg->key0, k1 = cfg->key1, ch = cfg->chain, sw = r->sw;
+  double *spatcoef = r->spatcoef, *phi = r->phi, bw = r->bw, nu = r->nu;
+  double wmr = 0.0;
+  for (int j = r->j0; j < r->j1; ++j) {
+    int vox = pb->vox[c][j], v = pb->idx[vox], sc = pb->idxsc[vox];
+    double bwm = bw * pb->wm[v];
+    double b[16] = {0}, e[16], zs = 0.0, qw[256] = {0};
+    uint32_t o[4];
+    for (int i = 0; i < N; ++i) {
+      if ((i & 3) == 0)
+        philox((uint32_t)(i >> 2), (uint32_t)v, sw, (ch << 8) | ORC_TAG_Z, k0, k1, o);
+      double mu = bwm;
+      for (int p = 0; p < P; ++p)
+        mu += spatcoef[(size_t)p * Vp + sc] * pb->covar[p * N + i];
+      int y = pb->data[(size_t)i * V + v] == 1;
+      /* t/logit links: (Z - mu) sqrt(phi) ~ N(0, 1) truncated */
+      double ph = r->mix ? phi[(size_t)i * V + v] : 1.0, sq = sqrt(ph);
+      double a = (y ? -mu : mu) * sq, t;
+      if (a <= ORC_A_TAIL) {
+        t = orc_tn_lower_inv(a, o[i & 3]);
+      } else {
+        uint32_t kp[2 * ORC_TAIL_MAX];
+        for (int q = 0; q < ORC_TAIL_MAX / 2; ++q)
+          philox((uint32_t)i * 8u + (uint32_t)q, (uint32_t)v, sw,
+                 (ch << 8) | ORC_TAG_ZTAIL, k0, k1, kp + 4 * q);
+        if (!orc_tn_lower_tail(a, kp, ORC_TAIL_MAX, &t)) err |= ORC_ERR_TN_CAP;
+      }
+      double rr = (y ? t : -t) / sq, z = mu + rr;
+      zs += z;
+      if (r->mix) {
+        double g = mix_gamma(cfg, r->md, r->mc, (uint32_t)i, (uint32_t)v, sw, &err);
+        double phn = 2.0 * g / (nu + rr * rr);
+        phi[(size_t)i * V + v] = phn;
+        for (int p = 0; p < P; ++p) {
+          double xp = pb->covar[p * N + i];
+          b[p] += xp * phn * (z - bwm);
+          for (int q = 0; q < P; ++q) qw[q + p * P] += phn * xp * pb->covar[q * N + i];
+        }
+      } else {
+        for (int p = 0; p < P; ++p) b[p] += pb->covar[p * N + i] * (z - bwm);
+      }
+    }
+    for (int p = 0; p < P; p += 4) {
+      philox((uint32_t)(p >> 2), (uint32_t)v, sw, (ch << 8) | ORC_TAG_BETA, k0, k1, o);
+      for (int q = 0; q < 4 && p + q < P; ++q) e[p + q] = orc_normal_from_bits(o[q]);
+    }
+    if (!beta_voxel(pb, c, j, b, r->omega, e, 1, spatcoef, r->mix ? qw : NULL))
+      err |= ORC_ERR_CHOL;
+    double xb = 0.0;
+    for (int p = 0; p < P; ++p) xb += r->xsum[p] * spatcoef[(size_t)p * Vp + sc];
+    wmr += pb->wm[v] * (zs - xb);
+  }
+  r->wmr = wmr;
+  r->err = err;
+}
+
+static void *chain_range_thread(void *arg) {
+  chain_colour_range((chain_range *)arg);
+  return NULL;
+}
+
 int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
                   int64_t nsweeps, double *spatcoef, double *omega,
                   double *acc_sum, double *acc_sq, double *prb_sum,
@@ -732,77 +820,60 @@ int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
   const int mix = cfg->model != 1 && phi;
   const double nu = cfg->t_df, md = 0.5 * (nu + 1.0) - 1.0 / 3.0;
   const double mc = 1.0 / sqrt(9.0 * md);
-  uint32_t k0 = cfg->key0, k1 = cfg->key1, ch = cfg->chain;
   double *prb = (double *)malloc(sizeof(double) * ((size_t)S * V + 1));
   double bw = beta_wm ? *beta_wm : cfg->beta_wm;
   double xsum[16] = {0}, wm2 = 0.0;
+  const int nth = g_orc_threads;
+  chain_range rg[256];
+  pthread_t tid[256];
   for (int p = 0; p < P; ++p)
     for (int i = 0; i < N; ++i) xsum[p] += pb->covar[p * N + i];
   for (int v = 0; v < V; ++v) wm2 += (double)pb->wm[v] * pb->wm[v];
   for (int64_t s = s0; s < s0 + nsweeps; ++s) {
     uint32_t sw = (uint32_t)s;
     double wmr = 0.0; /* sum_v WM_v sum_i (Z_iv - x_i' beta_v), new beta */
-    for (int c = 0; c < 2; ++c)
-      for (int j = 0; j < pb->n[c]; ++j) {
-        int vox = pb->vox[c][j], v = pb->idx[vox], sc = pb->idxsc[vox];
-        double bwm = bw * pb->wm[v];
-        double b[16] = {0}, e[16], zs = 0.0, qw[256] = {0};
-        uint32_t o[4];
-        for (int i = 0; i < N; ++i) {
-          if ((i & 3) == 0)
-            philox((uint32_t)(i >> 2), (uint32_t)v, sw,
-                   (ch << 8) | ORC_TAG_Z, k0, k1, o);
-          double mu = bwm;
-          for (int p = 0; p < P; ++p)
-            mu += spatcoef[(size_t)p * Vp + sc] * pb->covar[p * N + i];
-          int y = pb->data[(size_t)i * V + v] == 1;
-          /* t/logit links: (Z - mu) sqrt(phi) ~ N(0, 1) truncated */
-          double ph = mix ? phi[(size_t)i * V + v] : 1.0, sq = sqrt(ph);
-          double a = (y ? -mu : mu) * sq, t;
-          if (a <= ORC_A_TAIL) {
-            t = orc_tn_lower_inv(a, o[i & 3]);
-          } else {
-            uint32_t kp[2 * ORC_TAIL_MAX];
-            for (int q = 0; q < ORC_TAIL_MAX / 2; ++q)
-              philox((uint32_t)i * 8u + (uint32_t)q, (uint32_t)v, sw,
-                     (ch << 8) | ORC_TAG_ZTAIL, k0, k1, kp + 4 * q);
-            if (!orc_tn_lower_tail(a, kp, ORC_TAIL_MAX, &t))
-              err |= ORC_ERR_TN_CAP;
-          }
-          double r = (y ? t : -t) / sq, z = mu + r;
-          zs += z;
-          if (mix) {
-            double g = mix_gamma(cfg, md, mc, (uint32_t)i, (uint32_t)v, sw, &err);
-            double phn = 2.0 * g / (nu + r * r);
-            phi[(size_t)i * V + v] = phn;
-            for (int p = 0; p < P; ++p) {
-              double xp = pb->covar[p * N + i];
-              b[p] += xp * phn * (z - bwm);
-              for (int q = 0; q < P; ++q) qw[q + p * P] += phn * xp * pb->covar[q * N + i];
-            }
-          } else {
-            for (int p = 0; p < P; ++p) b[p] += pb->covar[p * N + i] * (z - bwm);
-          }
-        }
-        for (int p = 0; p < P; p += 4) {
-          philox((uint32_t)(p >> 2), (uint32_t)v, sw, (ch << 8) | ORC_TAG_BETA,
-                 k0, k1, o);
-          for (int r = 0; r < 4 && p + r < P; ++r)
-            e[p + r] = orc_normal_from_bits(o[r]);
-        }
-        if (!beta_voxel(pb, c, j, b, omega, e, 1, spatcoef, mix ? qw : NULL))
-          err |= ORC_ERR_CHOL;
-        double xb = 0.0;
-        for (int p = 0; p < P; ++p) xb += xsum[p] * spatcoef[(size_t)p * Vp + sc];
-        wmr += pb->wm[v] * (zs - xb);
+    for (int c = 0; c < 2; ++c) {
+      int n = pb->n[c], nt = nth < n ? nth : (n > 0 ? n : 1);
+      for (int t = 0; t < nt; ++t) {
+        chain_range *r = &rg[t];
+        r->pb = pb;
+        r->cfg = cfg;
+        r->spatcoef = spatcoef;
+        r->phi = phi;
+        r->omega = omega;
+        r->xsum = xsum;
+        r->bw = bw;
+        r->md = md;
+        r->mc = mc;
+        r->nu = nu;
+        r->mix = mix;
+        r->c = c;
+        r->sw = sw;
+        r->j0 = (int)((int64_t)n * t / nt);
+        r->j1 = (int)((int64_t)n * (t + 1) / nt);
       }
+      if (nt == 1) {
+        chain_colour_range(&rg[0]);
+      } else {
+        int started = 0;
+        for (int t = 1; t < nt; ++t, ++started)
+          if (pthread_create(&tid[t], NULL, chain_range_thread, &rg[t]) != 0) break;
+        chain_colour_range(&rg[0]);
+        for (int t = 1; t <= started; ++t) pthread_join(tid[t], NULL);
+        for (int t = started + 1; t < nt; ++t) chain_colour_range(&rg[t]);
+      }
+      for (int t = 0; t < nt; ++t) {
+        wmr += rg[t].wmr;
+        err |= rg[t].err;
+      }
+    }
     /* beta_WM | Z, beta (updateBetaGPU, covarGPU.cu:680-720): normal with
      * variance 1 / (N sum WM^2) and mean variance * wmr; the lesion
      * probabilities of this sweep use the beta_WM of its latent draws. */
     double bw_used = bw;
     if (cfg->wm_update) {
       uint32_t o[4];
-      philox(0u, 0u, sw, (ch << 8) | ORC_TAG_WM, k0, k1, o);
+      philox(0u, 0u, sw, (cfg->chain << 8) | ORC_TAG_WM, cfg->key0, cfg->key1, o);
       double var = 1.0 / ((double)N * wm2);
       bw = (double)(float)(var * wmr + sqrt(var) * orc_normal_from_bits(o[0]));
     }

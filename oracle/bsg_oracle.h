@@ -130,6 +130,9 @@ int orc_chain_run(const orc_problem *pb, const orc_chain_cfg *cfg, int64_t s0,
                   int64_t *nkept, double *beta_wm, double *wm_sum,
                   double *phi);
 
+/* Host threads orc_chain_run splits each colour's voxels over (default 1). */
+void orc_set_threads(int n);
+
 /* The scale-mixture Gamma(alpha, 1) draw of subject i at voxel v (the
  * counters and Marsaglia-Tsang test the GPU uses). */
 double orc_mix_gamma(double alpha, uint32_t i, uint32_t v, uint32_t sweep,

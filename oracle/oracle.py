@@ -13,6 +13,7 @@ this module.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
@@ -28,6 +29,14 @@ _d = C.c_double
 _i = C.c_int
 _i64 = C.c_int64
 _u32 = C.c_uint32
+
+
+def reference_tree() -> Path:
+    """The reference source tree the recipe compiles from: BSGLMM_REF if
+    set, else the recipe's default (`make print-ref`)."""
+    out = subprocess.run(["make", "-s", "-C", str(HERE), "print-ref"],
+                         capture_output=True, text=True, check=True).stdout
+    return Path(out.strip())
 
 
 def build_oracle(ref: bool = False) -> None:
@@ -75,6 +84,7 @@ def lib() -> C.CDLL:
             "orc_predict": (None, [_P, _d, _P, _P, _i, _d]),
             "orc_dic_de": (_d, [_P, _P, _P, _i]),
             "orc_mix_gamma": (_d, [_d, _u32, _u32, _u32, _u32, _u32, _u32]),
+            "orc_set_threads": (None, [_i]),
             "orc_chain_run": (_i, [_P, _P, _i64, _i64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
             "orc_port_new": (_P, [_P, C.c_uint64, _i]),
             "orc_port_free": (None, [_P]),
@@ -85,6 +95,8 @@ def lib() -> C.CDLL:
             f = getattr(L, k)
             f.restype = r
             f.argtypes = a
+        # the FP64 chain splits each colour's voxels over the host's cores
+        L.orc_set_threads(min(os.cpu_count() or 1, 64))
         _O = L
     return _O
 

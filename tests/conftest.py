@@ -33,3 +33,17 @@ def oracle_mod():
     import oracle
     oracle.build_oracle()
     return oracle
+
+
+def omega_rel_err(om, ref, tiny: float = 1e-2) -> float:
+    """Worst elementwise relative error of a precision matrix against its
+    reference over the entries that are not tiny (|ref| >= tiny * max|ref|);
+    the tiny ones are measured against tiny * max|ref| instead.  (The
+    reference forms Omega from FP32 pair sums and stores it in FP32, so its
+    near-zero off-diagonal entries carry an absolute rounding of about
+    1e-8 max|Omega|: an exact FP64 restatement differs from it by 7e-5
+    relative on an entry of 2e-4 max|Omega|.)"""
+    om = np.asarray(om, np.float64)
+    ref = np.asarray(ref, np.float64)
+    scale = np.maximum(np.abs(ref), tiny * np.abs(ref).max())
+    return float((np.abs(om - ref) / scale).max())

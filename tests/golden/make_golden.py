@@ -8,7 +8,12 @@ reference's outputs of one sweep in the reference's order
 (updateZ -> updateSpatCoef -> updateSpatCoefPrec, mcmc.cpp:400-428) plus
 compute_prb (covar.cpp:350-364) of the new state.
 
-Run from the repository root:  python tests/golden/make_golden.py
+The "c0" fixture is the benchmark's CPU-runnable study at full size (20^3
+grid, sphere r = 9 about (10.5, 10.5, 10.5), N = 50, P = 3); its latent Z
+(N V values) is left out to keep the file small.
+
+Run from the repository root:  python tests/golden/make_golden.py [name ...]
+(no names: every fixture).
 """
 from __future__ import annotations
 
@@ -35,6 +40,7 @@ def cases():
     st = synth.small_study(9, shape=(7, 8, 9), N=45, P=3, S=2)
     wm = np.random.default_rng(9).uniform(0.05, 1.0, st.V).astype(np.float32)
     yield "wm_p3", st, wm, 0.4
+    yield "c0", synth.config0(0), None, 0.0
 
 
 def _sphere():
@@ -76,18 +82,19 @@ def make(name, st, wm, beta_wm, seed):
         wm=wm if wm is not None else np.zeros(0, np.float32),
         beta_wm=np.float32(beta_wm), beta0=beta0, omega0=omega0, ubits=ubits,
         normals=normals, chi2=chi2, wnorm=wnorm, df_offset=np.int32(pb.P),
-        ref_Z=Z, ref_beta1=b1, ref_omega1=om1, ref_prb1=prb1,
+        ref_Z=np.zeros(0) if name == "c0" else Z, ref_beta1=b1, ref_omega1=om1, ref_prb1=prb1,
         idx=lat["idx"], idxsc=lat["idxsc"], vox0=lat["vox"][0],
         vox1=lat["vox"][1], nbrs0=lat["nbrs"][0], nbrs1=lat["nbrs"][1])
     np.savez_compressed(OUT / f"sweep_{name}.npz", **arrays)
     print(f"sweep_{name}.npz  V={pb.V} Vp={pb.Vp} N={pb.N} P={pb.P}")
 
 
-def main():
+def main(names):
     O.build_oracle(ref=True)
     for k, (name, st, wm, bwm) in enumerate(cases()):
-        make(name, st, wm, bwm, 100 + k)
+        if not names or name in names:
+            make(name, st, wm, bwm, 100 + k)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -11,7 +11,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import golden_cases, load_golden
+from conftest import golden_cases, load_golden, omega_rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -60,7 +60,10 @@ def test_supplied_sweep_matches_reference(bsg, name):
     assert np.allclose(b1, g["ref_beta1"], rtol=RTOL, atol=ATOL), \
         np.abs(b1 - g["ref_beta1"]).max()
     ref_om = g["ref_omega1"].astype(np.float64)
-    assert np.allclose(om1, ref_om, rtol=RTOL, atol=ATOL * np.abs(ref_om).max())
+    # elementwise relative, entries below 1e-2 max|Omega| against that floor
+    worst = omega_rel_err(om1, ref_om)
+    print(f"{name}: worst Omega relative error {worst:.3g}")
+    assert worst <= RTOL, worst
     prb = s.compute_prb(ch)
     assert np.allclose(prb, g["ref_prb1"], atol=2e-6)
     assert s.sweep_count(ch) == (1, 0)
@@ -84,7 +87,9 @@ def test_supplied_sweep_production_form(bsg, oracle_mod, name):
     assert fails == 0 and ok
     b1 = s.beta(ch)
     assert np.allclose(b1, ob, rtol=RTOL, atol=ATOL), np.abs(b1 - ob).max()
-    assert np.allclose(s.omega(ch), oom, rtol=RTOL, atol=ATOL * np.abs(oom).max())
+    worst = omega_rel_err(s.omega(ch), oom)
+    print(f"{name}: worst Omega relative error {worst:.3g}")
+    assert worst <= RTOL, worst
     assert np.allclose(s.colmeans(ch), pb.col_means(b1.astype(np.float64)),
                        rtol=RTOL, atol=ATOL)
     s.close()

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 from scipy import special, stats
 
-from conftest import golden_cases, load_golden
+from conftest import golden_cases, load_golden, omega_rel_err
 
 # Published Philox-4x32-10 known-answer vectors (Random123 KAT set).
 PHILOX_KAT = [
@@ -118,9 +118,10 @@ def test_oracle_matches_reference_golden(oracle_mod, name):
         g["beta0"].astype(np.float64), g["omega0"].astype(np.float64), g["ubits"],
         g["normals"], g["chi2"], g["wnorm"], form=0, beta_wm=bwm)
     assert fails == 0 and ok
-    assert np.allclose(Z, g["ref_Z"], rtol=1e-5, atol=1e-5)
+    if g["ref_Z"].size:  # (left out of the largest fixture)
+        assert np.allclose(Z, g["ref_Z"], rtol=1e-5, atol=1e-5)
     assert np.allclose(b, g["ref_beta1"], rtol=1e-5, atol=1e-5)
-    assert np.allclose(om, g["ref_omega1"], rtol=1e-5, atol=1e-5 * np.abs(om).max())
+    assert omega_rel_err(om, g["ref_omega1"]) <= 1e-5
     prb = pb.compute_prb(g["ref_beta1"].astype(np.float64), bwm)
     assert np.allclose(prb, g["ref_prb1"], atol=1e-6)
 

@@ -10,8 +10,10 @@ from pathlib import Path
 
 import pytest
 
+import oracle
+
 ROOT = Path(__file__).resolve().parents[1]
-REF = Path("/root/reference/bsglmm")
+REF = oracle.reference_tree()
 
 
 def _nm(obj: Path, flag: str) -> set[str]:

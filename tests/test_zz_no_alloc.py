@@ -8,11 +8,16 @@ device.  The caller passes device buffers it already owns; the reduction's
 scratch comes from a fixed array inside the library.
 
 The test calls it through the C ABI and checks its Omega against the one
-the sampler's own post-sweep pass (bsg_sweep_supplied / bsg_run) draws from
+the sampler draws at the end of a sweep (bsg_sweep_supplied / bsg_run) from
 the same beta and variates, on two calls in a row so that the second call
-runs on the scratch the first one left behind.  Device buffers for the test
-come from torch; the entry point itself allocates nothing.  This file is
-collected last so a failure here does not hide the other GPU tests.
+runs on the scratch the first one left behind.  The two are computed
+differently -- this entry point sums the pair products per thread in FP64
+and factors by chol -> invert -> chol, the sampler sums them in FP32 warp
+trees and uses a reverse Cholesky -- so they agree to rounding, checked at
+1e-5 relative.  Device buffers for the test come from torch; the entry point
+itself allocates nothing, which the last test checks through the device's
+free memory around a call.  This file is collected last so a failure here
+does not hide the other GPU tests.
 """
 from __future__ import annotations
 
@@ -99,6 +104,41 @@ def test_noalloc_matches_sampler_with_philox_variates():
                                        chain=ch, sweep=sweep)
             assert status == 0 and err == 0, (call, status, err)
             assert np.allclose(om, om_ref, rtol=RTOL, atol=ATOL * np.abs(om_ref).max()), call
+
+
+def test_noalloc_call_leaves_device_memory_unchanged():
+    """After a first call (which loads the module), a further call takes no
+    device memory: cudaMemGetInfo's free bytes are the same before and
+    after it, with every buffer allocated beforehand."""
+    torch = pytest.importorskip("torch")
+    import bsglmm_gb300 as bsg
+    st = _study()
+    with bsg.Sampler() as s:
+        L = s._L
+        ds = s.add_dataset(st.mask, st.covar, st.data, 1)
+        ch = s.add_chain(ds, seed=5)
+        s.run(1)
+        P = s.info(ds)["P"]
+        info, lat = s.info(ds), s.lattice(ds)
+        vox = torch.from_numpy(np.concatenate(lat["vox"])).cuda()
+        idxsc = torch.from_numpy(lat["idxsc"]).cuda()
+        d_beta = torch.from_numpy(np.ascontiguousarray(s.beta(ch))).cuda()
+        d_om = torch.zeros((P, P), dtype=torch.float64, device="cuda")
+        d_st = torch.zeros((1,), dtype=torch.int32, device="cuda")
+
+        def call():
+            return L.bsg_omega_update_noalloc(
+                _ptr(d_beta), _ptr(vox), _ptr(idxsc), info["X"], info["Y"], info["V"],
+                info["Vp"], P, P, None, None, 5, ch, 0, _ptr(d_om), _ptr(d_st), None)
+
+        assert call() == 0
+        torch.cuda.synchronize()
+        free0, _ = torch.cuda.mem_get_info()
+        assert call() == 0
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        assert int(d_st.cpu()[0]) == 0
+        assert free1 == free0, (free0, free1)
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch():

@@ -56,6 +56,8 @@ SIGNATURES = {
     "bsg_set_predictive": (_i32, [_P, _i32, _i32]),
     "bsg_set_wm_update": (_i32, [_P, _i32, _i32]),
     "bsg_set_model": (_i32, [_P, _i32, _i32]),
+    "bsg_set_precision": (_i32, [_P, _i32, _i32]),
+    "bsg_get_beta64": (_i32, [_P, _i32, _P]),
     "bsg_get_beta_wm": (_i32, [_P, _i32, C.POINTER(C.c_float), C.POINTER(C.c_double)]),
     "bsg_predict": (_i32, [_P, _i32, _P]),
     "bsg_get_predictive": (_i32, [_P, _i32, _P, C.POINTER(C.c_double),

@@ -29,13 +29,15 @@ SOURCES = [
     "bsg_fused_l8.cu",
     "bsg_fused_mix.cu",
     "bsg_fused_wm.cu",
+    "bsg_fp64.cu",
     "bsg_kernels.cu",
     "bsg_peak.cu",
     "bsg_noalloc.cu",
     "bsg_predict.cu",
     "bsg_api.cpp",
 ]
-HEADERS = ["bsg_device.cuh", "bsg_fused.cuh", "bsg_internal.h", "bsg_math.cuh"]
+HEADERS = ["bsg_device.cuh", "bsg_fused.cuh", "bsg_internal.h", "bsg_math.cuh",
+           "bsg_wishart.cuh"]
 
 
 def nvcc() -> str:

@@ -45,6 +45,7 @@ struct Group {
   int P = 0;
   bool mix = false;     // t/logit chains (scale-mixture colour kernel)
   bool wm_any = false;  // its chains draw beta_WM: colour 0 waits for it
+  bool fp64 = false;    // FP64 chains (fp64_colour_kernel, no early start)
   std::vector<BlockMap> map[2];
   BlockMap *d_map[2] = {nullptr, nullptr};
   // predictive pass of the group's chains that have it on, one launch pair
@@ -318,8 +319,8 @@ bsg_status build_plan(bsg_ctx *ctx) {
   }
   const int vpb = ctx->threads / ctx->lpv;
   // partial rows for the smallest tile any kernel of this context uses
-  bsg_status ps =
-      ensure_partials(ctx, std::min({vpb, kParityThreads, ctx->threads / kMixLpv}));
+  bsg_status ps = ensure_partials(
+      ctx, std::min({vpb, kParityThreads, ctx->threads / kMixLpv, kF64Threads}));
   if (ps) return ps;
   std::vector<DatasetDev> hds;
   for (auto &d : ctx->ds) hds.push_back(d.dev);
@@ -339,18 +340,22 @@ bsg_status build_plan(bsg_ctx *ctx) {
     const Dataset &d = ctx->ds[ctx->ch[ci].dataset];
     const bool mix = ctx->ch[ci].dev.model != 1;
     const bool wmu = ctx->ch[ci].dev.wm_update != 0;
+    const bool f64 = ctx->ch[ci].dev.fp64 != 0;
     Group *g = nullptr;
     for (auto &gg : ctx->groups)
-      if (gg.P == d.P && gg.mix == mix && gg.wm_any == wmu) g = &gg;
+      if (gg.P == d.P && gg.mix == mix && gg.wm_any == wmu && gg.fp64 == f64) g = &gg;
     if (!g) {
       ctx->groups.push_back(Group());
       g = &ctx->groups.back();
       g->P = d.P;
       g->mix = mix;
       g->wm_any = wmu;
+      g->fp64 = f64;
     }
-    // the t/logit kernel runs kMixLpv lanes per voxel, the beta_WM one one
-    const int gvpb = mix ? ctx->threads / kMixLpv : (wmu ? ctx->threads : vpb);
+    // the t/logit kernel runs kMixLpv lanes per voxel, the beta_WM one one,
+    // the FP64 one one thread per voxel in blocks of kF64Threads
+    const int gvpb = f64 ? kF64Threads
+                         : (mix ? ctx->threads / kMixLpv : (wmu ? ctx->threads : vpb));
     for (int c = 0; c < 2; ++c) map_chain(g->map[c], (int)ci, (int)d.vox[c].size(), gvpb, c);
     if (ctx->ch[ci].pred_on) {
       const ChainDev &cv = ctx->ch[ci].dev;
@@ -396,6 +401,9 @@ bsg_status build_plan(bsg_ctx *ctx) {
 // kernel also reduces the Omega pairs and draws Omega.
 // One colour kernel of a group.
 cudaError_t launch_colour(bsg_ctx *ctx, const Group &g, int c, cudaStream_t st, bool pdl) {
+  if (g.fp64)
+    return launch_fp64(g.P, ctx->d_ds, ctx->d_ch, g.d_map[c], (int)g.map[c].size(), c,
+                       st);
   if (g.mix)
     return launch_fused_mix(g.P, ctx->threads, ctx->d_ds, ctx->d_ch, g.d_map[c],
                             (int)g.map[c].size(), c, st, pdl);
@@ -412,7 +420,7 @@ cudaError_t enqueue_group(bsg_ctx *ctx, const Group &g, cudaStream_t st) {
   for (int c = 0; c < 2; ++c) {
     // the colour-0 latent phase reads beta_WM, which the previous colour-1
     // kernel draws when the update is on: no early start then
-    const bool pdl = ctx->pdl && !(c == 0 && g.wm_any);
+    const bool pdl = ctx->pdl && !(c == 0 && g.wm_any) && !g.fp64;
     e = launch_colour(ctx, g, c, st, pdl);
     if (e != cudaSuccess) return e;
   }
@@ -555,6 +563,28 @@ bsg_status set_model(bsg_ctx *ctx, Chain &c, int model) {
   return BSG_OK;
 }
 
+// Turns a chain's FP64 mode on or off.  On: the FP64 coefficients start
+// from the current float ones.  Off: the float copy (kept in step by the
+// FP64 kernel) simply carries on.
+bsg_status set_precision(bsg_ctx *ctx, Chain &c, int bits) {
+  const Dataset &d = ctx->ds[c.dataset];
+  const size_t n = (size_t)d.P * d.Vp;
+  cudaError_t e;
+  if (bits == 64) {
+    if (!c.dev.beta64) {
+      c.dev.beta64 = (double *)dalloc(ctx, sizeof(double) * n, &e);
+      CK(e);
+    }
+    std::vector<float> bf(n);
+    CK(d2h(ctx, bf.data(), c.dev.beta, sizeof(float) * n));
+    std::vector<double> bd(bf.begin(), bf.end());
+    CK(h2d(ctx, c.dev.beta64, bd.data(), sizeof(double) * n));
+  }
+  const int32_t on = bits == 64 ? 1 : 0;
+  if (c.dev.fp64 != on) ctx->plan_valid = false;
+  c.dev.fp64 = on;
+  return BSG_OK;
+}
 }  // namespace
 
 // ========================================================================
@@ -973,7 +1003,8 @@ int64_t bsg_launches_per_sweep(const bsg_ctx *ctx) {
   std::vector<int> ps, pp;
   for (auto &c : ctx->ch) {
     const Dataset &d = ctx->ds[c.dataset];
-    const int P = d.P * 4 + (c.dev.model != 1) * 2 + (c.dev.wm_update != 0);
+    const int P = d.P * 8 + (c.dev.model != 1) * 2 + (c.dev.wm_update != 0) +
+                  (c.dev.fp64 != 0) * 4;
     const int PS = d.P * 16 + d.S;
     if (std::find(ps.begin(), ps.end(), P) == ps.end()) ps.push_back(P);
     if (c.pred_on && std::find(pp.begin(), pp.end(), PS) == pp.end()) pp.push_back(PS);
@@ -1031,6 +1062,10 @@ bsg_status bsg_set_beta(bsg_ctx *ctx, int32_t chain, const float *in) {
       if (!inmask[s]) b[(size_t)p * d.Vp + s] = 0.f;
   CK(cudaSetDevice(ctx->device));
   CK(h2d(ctx, c.dev.beta, b.data(), sizeof(float) * b.size()));
+  if (c.dev.fp64) {  // the FP64 chain's own coefficients follow
+    std::vector<double> bd(b.begin(), b.end());
+    CK(h2d(ctx, c.dev.beta64, bd.data(), sizeof(double) * bd.size()));
+  }
   return BSG_OK;
 }
 
@@ -1076,6 +1111,8 @@ bsg_status bsg_set_wm_update(bsg_ctx *ctx, int32_t chain, int32_t enable) {
     return fail(ctx, BSG_ERR_INVALID, "the beta_WM update needs a nonzero WM map");
   if (enable && c.dev.model != 1)
     return fail(ctx, BSG_ERR_UNSUPPORTED, "the beta_WM update is probit only");
+  if (enable && c.dev.fp64)
+    return fail(ctx, BSG_ERR_UNSUPPORTED, "FP64 chains keep beta_WM fixed");
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   const int32_t on = enable ? 1 : 0;
@@ -1245,34 +1282,38 @@ size_t ckpt_bytes_v1(const Dataset &d) {
 }
 
 struct MixCkpt {  // link (MODEL); its weights phi follow unless probit
-  int32_t model, pad;
+  int32_t model;
+  int32_t bits;     // 64: an FP64 chain, whose beta64 [P][Vp] follows (0 = 32)
 };
 
 // Version 2 layout: the v1 body, PredCkpt, Qhat [N][max(S,1)], WmCkpt,
-// MixCkpt, then phi [N][n_0] and [N][n_1] for the t/logit links.
+// MixCkpt, then phi [N][n_0] and [N][n_1] for the t/logit links, then the
+// FP64 coefficients of an FP64 chain.
 size_t ckpt_fixed(const Dataset &d) {
   return ckpt_bytes_v1(d) + sizeof(PredCkpt) +
          sizeof(double) * (size_t)d.N * std::max(d.S, 1) + sizeof(WmCkpt) +
          sizeof(MixCkpt);
 }
 
-size_t ckpt_bytes(const Dataset &d, int model) {
-  return ckpt_fixed(d) + (model != 1 ? sizeof(float) * (size_t)d.N *
-                                           (d.vox[0].size() + d.vox[1].size())
-                                     : 0);
+size_t ckpt_bytes(const Dataset &d, int model, bool fp64) {
+  return ckpt_fixed(d) +
+         (model != 1 ? sizeof(float) * (size_t)d.N * (d.vox[0].size() + d.vox[1].size())
+                     : 0) +
+         (fp64 ? sizeof(double) * (size_t)d.P * d.Vp : 0);
 }
 }  // namespace
 
 int64_t bsg_checkpoint_size(const bsg_ctx *ctx, int32_t chain) {
   if (!valid_chain(ctx, chain)) return -1;
-  return (int64_t)ckpt_bytes(ctx->ds[ctx->ch[chain].dataset], ctx->ch[chain].dev.model);
+  const Chain &c = ctx->ch[chain];
+  return (int64_t)ckpt_bytes(ctx->ds[c.dataset], c.dev.model, c.dev.fp64 != 0);
 }
 
 bsg_status bsg_checkpoint(bsg_ctx *ctx, int32_t chain, void *buf, int64_t size) {
   if (!valid_chain(ctx, chain) || !buf) return BSG_ERR_INVALID;
   const Chain &c = ctx->ch[chain];
   const Dataset &d = ctx->ds[c.dataset];
-  if (size < (int64_t)ckpt_bytes(d, c.dev.model))
+  if (size < (int64_t)ckpt_bytes(d, c.dev.model, c.dev.fp64 != 0))
     return fail(ctx, BSG_ERR_INVALID, "buffer too small");
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -1311,12 +1352,13 @@ bsg_status bsg_checkpoint(bsg_ctx *ctx, int32_t chain, void *buf, int64_t size) 
   const WmCkpt wk{c.dev.wm_update, 0, ws.sum};
   std::memcpy(p, &wk, sizeof(wk));
   p += sizeof(wk);
-  const MixCkpt mk{c.dev.model, 0};
+  const MixCkpt mk{c.dev.model, c.dev.fp64 ? 64 : 0};
   std::memcpy(p, &mk, sizeof(mk));
   p += sizeof(mk);
   if (c.dev.model != 1)
     for (int k = 0; k < 2; ++k)
       CK(get(c.dev.phi[k], sizeof(float) * (size_t)d.N * d.vox[k].size()));
+  if (c.dev.fp64) CK(get(c.dev.beta64, sizeof(double) * (size_t)d.P * d.Vp));
   return BSG_OK;
 }
 
@@ -1336,7 +1378,9 @@ bsg_status bsg_restore(bsg_ctx *ctx, int32_t chain, const void *buf, int64_t siz
   if (h.version == 2) {
     std::memcpy(&mk, static_cast<const char *>(buf) + ckpt_fixed(d) - sizeof(MixCkpt),
                 sizeof(mk));
-    if (mk.model < 0 || mk.model > 2 || size < (int64_t)ckpt_bytes(d, mk.model))
+    if (mk.model < 0 || mk.model > 2 || (mk.bits != 0 && mk.bits != 64) ||
+        (mk.bits == 64 && mk.model != 1) ||
+        size < (int64_t)ckpt_bytes(d, mk.model, mk.bits == 64))
       return fail(ctx, BSG_ERR_INVALID, "checkpoint is for a study of another shape");
   }
   CK(cudaSetDevice(ctx->device));
@@ -1397,6 +1441,11 @@ bsg_status bsg_restore(bsg_ctx *ctx, int32_t chain, const void *buf, int64_t siz
   if (mk.model != 1)
     for (int k = 0; k < 2; ++k)
       CK(put(c.dev.phi[k], sizeof(float) * (size_t)d.N * d.vox[k].size()));
+  {
+    bsg_status fs = set_precision(ctx, c, mk.bits == 64 ? 64 : 32);
+    if (fs) return fs;
+  }
+  if (mk.bits == 64) CK(put(c.dev.beta64, sizeof(double) * (size_t)d.P * d.Vp));
   c.desc.beta_wm = h.beta_wm;
   c.dev.df_offset = h.df_offset;
   c.dev.burnin = h.burnin;
@@ -1414,7 +1463,8 @@ bsg_status bsg_autotune(bsg_ctx *ctx, int32_t sweeps, int32_t *best_lpv,
   if (ctx->ch.empty()) return fail(ctx, BSG_ERR_STATE, "no chain");
   std::vector<std::vector<char>> saved(ctx->ch.size());
   for (size_t i = 0; i < ctx->ch.size(); ++i) {
-    saved[i].resize(ckpt_bytes(ctx->ds[ctx->ch[i].dataset], ctx->ch[i].dev.model));
+    saved[i].resize(ckpt_bytes(ctx->ds[ctx->ch[i].dataset], ctx->ch[i].dev.model,
+                               ctx->ch[i].dev.fp64 != 0));
     bsg_status s = bsg_checkpoint(ctx, (int32_t)i, saved[i].data(), (int64_t)saved[i].size());
     if (s) return s;
   }
@@ -1460,6 +1510,8 @@ bsg_status bsg_sweep_supplied(bsg_ctx *ctx, int32_t chain, const uint32_t *ubits
                 "supplied-variate sweeps take beta_WM as given (turn its update off)");
   if (c.dev.model != 1)
     return fail(ctx, BSG_ERR_UNSUPPORTED, "supplied-variate sweeps are probit only");
+  if (c.dev.fp64)
+    return fail(ctx, BSG_ERR_UNSUPPORTED, "supplied-variate sweeps run in FP32");
   cudaError_t e;
   const int P = d.P, nw = P * (P - 1) / 2;
   Supplied sup{};
@@ -1502,9 +1554,40 @@ bsg_status bsg_set_model(bsg_ctx *ctx, int32_t chain, int32_t model) {
   Chain &c = ctx->ch[chain];
   if (model != 1 && c.dev.wm_update)
     return fail(ctx, BSG_ERR_UNSUPPORTED, "the beta_WM update is probit only");
+  if (model != 1 && c.dev.fp64)
+    return fail(ctx, BSG_ERR_UNSUPPORTED, "FP64 chains are probit only");
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   return set_model(ctx, c, model);
+}
+
+// ------------------------------------------------------- FP64 chains ----
+bsg_status bsg_set_precision(bsg_ctx *ctx, int32_t chain, int32_t bits) {
+  if (!valid_chain(ctx, chain) || (bits != 32 && bits != 64)) return BSG_ERR_INVALID;
+  Chain &c = ctx->ch[chain];
+  if (bits == 64 && c.dev.model != 1)
+    return fail(ctx, BSG_ERR_UNSUPPORTED, "FP64 chains are probit only");
+  if (bits == 64 && c.dev.wm_update)
+    return fail(ctx, BSG_ERR_UNSUPPORTED, "FP64 chains keep beta_WM fixed");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return set_precision(ctx, c, bits);
+}
+
+bsg_status bsg_get_beta64(bsg_ctx *ctx, int32_t chain, double *out) {
+  if (!valid_chain(ctx, chain) || !out) return BSG_ERR_INVALID;
+  const Chain &c = ctx->ch[chain];
+  const Dataset &d = ctx->ds[c.dataset];
+  const size_t n = (size_t)d.P * d.Vp;
+  CK(cudaSetDevice(ctx->device));
+  if (c.dev.fp64) {
+    CK(d2h(ctx, out, c.dev.beta64, sizeof(double) * n));
+  } else {
+    std::vector<float> bf(n);
+    CK(d2h(ctx, bf.data(), c.dev.beta, sizeof(float) * n));
+    std::copy(bf.begin(), bf.end(), out);
+  }
+  return BSG_OK;
 }
 
 // ------------------------------------------------ DIC / Qhat predictive --

@@ -83,6 +83,14 @@ __device__ __forceinline__ double u_of_d(uint32_t k) {
   return ((double)k + 0.5) * 0x1p-32;
 }
 
+// Standard normal by inversion with exact tails, in FP64 (CUDA's
+// normcdfinv): the variates of the FP64 chain.
+__device__ __forceinline__ double normal_of_d(uint32_t k) {
+  const bool lo = k < 0x80000000u;
+  const double t = normcdfinv(u_of_d(lo ? k : ~k));
+  return lo ? t : -t;
+}
+
 // Standard normal by inversion with exact tails.
 __device__ __forceinline__ float normal_of(uint32_t k) {
   const bool lo = k < 0x80000000u;

@@ -26,6 +26,7 @@ constexpr int kPostPerThread = 4;   // Omega pass (bsg_noalloc.cu)
 constexpr int kMaxThreads = 256;    // largest block of the colour kernel
 constexpr int kPredThreads = 128;   // subjects per block of the predictive pass
 constexpr int kPredWarps = 8;       // subjects (one warp each) per finishing block
+constexpr int kF64Threads = 128;    // voxels (one thread each) per FP64-chain block
 
 // Predictive-pass modes: after each kept sweep (ED and Qhat accumulate), on
 // demand (Mpredict of the current coefficients), or the DE deviance at the
@@ -88,6 +89,10 @@ struct ChainDev {
   float *phi[2];           // [N][n_c] per colour: weights (t/logit links)
   int32_t df_offset, burnin, thin;
   float *beta;             // [P][Vp]
+  // FP64 chain: the whole sweep in double precision on the same counters;
+  // beta64 holds the coefficients and beta a float copy of them
+  int32_t fp64;
+  double *beta64;          // [P][Vp] (FP64 chains only)
   float *omega_f;          // [P*P] float copy read by the colour kernels
   double *omega_d;         // [P*P]
   float *colmean;          // [P]
@@ -149,6 +154,10 @@ constexpr int kMixLpv = 2;
 cudaError_t launch_fused_mix(int P, int threads, const DatasetDev *ds, ChainDev *ch,
                              const BlockMap *map, int nblocks, int colour,
                              cudaStream_t st, bool pdl);
+// The colour kernel of FP64 chains (bsg_fp64.cu): one thread per voxel,
+// kF64Threads voxels per block, Philox variates, probit link.
+cudaError_t launch_fp64(int P, const DatasetDev *ds, ChainDev *ch, const BlockMap *map,
+                        int nblocks, int colour, cudaStream_t st);
 cudaError_t launch_prb(const DatasetDev *ds, const ChainDev *ch, int chain,
                        const DatasetDev &dh, float *prb, cudaStream_t st);
 cudaError_t launch_fill(float *p, size_t n, float value, cudaStream_t st);

@@ -12,7 +12,9 @@ namespace bsg {
 // Attempt t of slot uses counter (slot*64 + t, 0, sweep, chain<<8|GAMMA).
 // The squeeze u < 1 - 0.0331 x^4 lies inside the acceptance region, so it
 // accepts exactly the attempts the log test would; it spares the two FP64
-// logarithms in most attempts.
+// logarithms in most attempts.  F64: the normal of each attempt in FP64
+// (the FP64 chain) instead of the FP32 inversion.
+template <bool F64 = false>
 static __device__ double gamma_mt(double a, uint32_t slot, uint32_t sweep,
                                   uint32_t c3, uint32_t k0, uint32_t k1,
                                   int *err) {
@@ -22,7 +24,7 @@ static __device__ double gamma_mt(double a, uint32_t slot, uint32_t sweep,
   for (int t = 0; t < kGammaMax; ++t) {
     const uint4 r = philox1(make_uint4(slot * 64u + (uint32_t)t, 0u, sweep, c3),
                             k0, k1);
-    const double x = (double)normal_of(r.x);
+    const double x = F64 ? normal_of_d(r.x) : (double)normal_of(r.x);
     const double cx = c * x;
     if (!(cx > -1.0)) continue;
     const double v3 = (1.0 + cx) * (1.0 + cx) * (1.0 + cx);
@@ -39,7 +41,8 @@ static __device__ double gamma_mt(double a, uint32_t slot, uint32_t sweep,
 // draws sqrt(chi^2(df - i)) into wd[i], lane q < P(P-1)/2 the normal of
 // the q-th strictly lower entry (row-major) into wd[kMaxP + q].  Run by the
 // last colour-0 block, off the Omega draw's dependency chain.  Returns the
-// lane's error bits.
+// lane's error bits.  F64: normals in FP64 (the FP64 chain).
+template <bool F64 = false>
 static __device__ int wishart_draws(const ChainDev &ch, const DatasetDev &d,
                                     long long sweep, int lane, double *wd) {
   const int P = d.P;
@@ -47,12 +50,13 @@ static __device__ int wishart_draws(const ChainDev &ch, const DatasetDev &d,
   int err = 0;
   const double df = (double)d.V + (double)ch.df_offset;
   if (lane < P)
-    wd[lane] = sqrt(2.0 * gamma_mt(0.5 * (df - lane), (uint32_t)lane, sw,
-                                   cid | kTagGamma, ch.key0, ch.key1, &err));
+    wd[lane] = sqrt(2.0 * gamma_mt<F64>(0.5 * (df - lane), (uint32_t)lane, sw,
+                                        cid | kTagGamma, ch.key0, ch.key1, &err));
   if (lane < P * (P - 1) / 2) {
     const uint4 r = philox1(make_uint4((uint32_t)(lane >> 2), 0u, sw, cid | kTagWNorm),
                             ch.key0, ch.key1);
-    wd[kMaxP + lane] = (double)normal_of(pick4(r, lane & 3));
+    wd[kMaxP + lane] = F64 ? normal_of_d(pick4(r, lane & 3))
+                           : (double)normal_of(pick4(r, lane & 3));
   }
   return err;
 }

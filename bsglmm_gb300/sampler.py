@@ -240,6 +240,20 @@ class Sampler:
         m = self.MODELS[model] if isinstance(model, str) else int(model)
         self._check(self._L.bsg_set_model(self._h, chain, m), "bsg_set_model")
 
+    # ------------------------------------------------------ FP64 chains --
+    def set_precision(self, chain: int = 0, bits: int = 64):
+        """64: the chain's whole sweep in FP64 on the same counters (the GPU
+        reference chain); 32: the FP32 sampler (default)."""
+        self._check(self._L.bsg_set_precision(self._h, chain, int(bits)),
+                    "bsg_set_precision")
+
+    def beta64(self, chain: int = 0) -> np.ndarray:
+        """Coefficients [P][Vp] in FP64 (an FP64 chain's own)."""
+        d = self._dims(chain)
+        out = np.zeros((d["P"], d["Vp"]), np.float64)
+        self._check(self._L.bsg_get_beta64(self._h, chain, _ptr(out)), "bsg_get_beta64")
+        return out
+
     # ------------------------------------------------ beta_WM update --
     def set_wm_update(self, chain: int = 0, enable: bool = True):
         """Draw beta_WM | Z, beta every sweep (updateBetaGPU)."""

@@ -145,6 +145,20 @@ bsg_status bsg_set_wm_update(bsg_ctx *ctx, int32_t chain, int32_t enable);
  * The t/logit links take production (Philox) variates only and no beta_WM
  * update. */
 bsg_status bsg_set_model(bsg_ctx *ctx, int32_t chain, int32_t model);
+/* Arithmetic of a chain's sweep: 32 (default) is the FP32 sampler with FP64
+ * Omega and posterior sums; 64 runs the whole sweep in FP64 on the same
+ * Philox counters (latent draws with CUDA's double normcdf / normcdfinv,
+ * X'Z, the Cholesky and coefficient draw, the Omega pair sums and Bartlett
+ * variates, the A&S lesion probabilities), the scheme of the reference's
+ * CPU path (covar.cpp:121-325) and of the project's FP64 oracle chain.  It
+ * is the GPU reference chain that FP32 maps are measured against at sizes
+ * the CPU cannot run; it is several times slower than FP32.  Probit link
+ * with beta_WM fixed only (BSG_ERR_UNSUPPORTED otherwise); FP64 state is
+ * kept in checkpoints.  No counterpart in the reference. */
+bsg_status bsg_set_precision(bsg_ctx *ctx, int32_t chain, int32_t bits);
+/* The chain's coefficients in FP64 ([P][Vp]): an FP64 chain's own, else the
+ * FP32 ones widened. */
+bsg_status bsg_get_beta64(bsg_ctx *ctx, int32_t chain, double *spatcoef);
 /* Current beta_WM and its mean over kept sweeps (the bWM map of
  * mcmc.cpp:795-840 is that mean times WM_v).  Either pointer may be NULL. */
 bsg_status bsg_get_beta_wm(bsg_ctx *ctx, int32_t chain, float *beta_wm,

@@ -47,17 +47,42 @@ L2_FLUSH_BYTES = 512 << 20
 CPU_CAL_VOX = 2000      # voxels per colour of the CPU calibration sweep
 CPU_BASELINE_S = 10.0   # seconds of CPU work in the cpu_baseline sample
 CPU_REFERENCE_S = 90.0  # seconds of CPU work in a whole reference-arm run
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one colour
-# launch of the fused kernel on the brain-sized workload, the mean of the
-# colour-0 and colour-1 launches of one ncu capture (43.81 + 0.08 MB and
-# 43.89 + 0.09 MB).  ncu cannot run inside a timed bench, so the captured
-# figure is carried here and reported only for that workload.
-NCU_TRAFFIC_PER_LAUNCH = 43.935e6
-# Thread instructions per subject-voxel update of the same capture's colour
-# launches (smsp__inst_executed x 32 / updates, the mean of 60.1 and 60.6):
-# the issue-slot roofline below divides the instruction rate this implies
-# by the SMs' issue peak (4 warp instructions per clock per SM).
-NCU_INST_PER_UPDATE = 60.35
+# The ncu figures of the fused colour kernel on the brain-sized workload
+# (DRAM bytes per colour launch, thread instructions per update) are read
+# from the committed profile summary, which records the hash of the kernel
+# sources it was captured on; the line says "stale" when the sources have
+# changed since.
+PROFILE = ROOT / "profiles" / "fused_colour_kernel_brain_c1.md"
+KERNEL_SOURCES = ["bsg_fused.cuh", "bsg_device.cuh", "bsg_math.cuh", "bsg_wishart.cuh",
+                  "bsg_internal.h", "bsg_fused_l1.cu"]
+
+
+def kernel_sources_hash() -> str:
+    import hashlib
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        h.update((ROOT / "bsglmm_gb300" / "csrc" / f).read_bytes())
+    return h.hexdigest()[:16]
+
+
+def profile_inputs() -> dict:
+    """The `bench-inputs` block of the profile summary: key: value lines
+    between '<!-- bench-inputs' and '-->'."""
+    out = {"source": str(PROFILE.relative_to(ROOT))}
+    try:
+        text = PROFILE.read_text()
+        block = text.split("<!-- bench-inputs", 1)[1].split("-->", 1)[0]
+    except (OSError, IndexError):
+        return out
+    for line in block.strip().splitlines():
+        k, _, v = line.partition(":")
+        v = v.strip()
+        try:
+            out[k.strip()] = float(v) if k.strip() != "kernel_sources_sha256" else v
+        except ValueError:
+            out[k.strip()] = v
+    out["stale"] = out.get("kernel_sources_sha256") != kernel_sources_hash()
+    return out
 
 
 def fused_flops_per_update(P: int) -> int:
@@ -141,11 +166,14 @@ class Clocks:
                 "sm_max_mhz": mx, "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def issue_roofline(device: int, updates_per_s: float):
+def issue_roofline(device: int, updates_per_s: float, prof: dict):
     """The binding resource of the colour kernel is issue slots: thread
     instructions per second (ncu's instructions per update x the live update
     rate of a colour launch) against 4 warp instructions per clock per SM at
     the maximum SM clock."""
+    ipu = prof.get("thread_inst_per_update")
+    if ipu is None:
+        return None
     try:
         import torch
         props = torch.cuda.get_device_properties(device)
@@ -156,11 +184,11 @@ def issue_roofline(device: int, updates_per_s: float):
             timeout=20).stdout.strip().splitlines()[0])
     except Exception:
         return None
-    achieved = NCU_INST_PER_UPDATE * updates_per_s / 1e12
+    achieved = ipu * updates_per_s / 1e12
     peak = 4 * 32 * sms * mhz * 1e6 / 1e12
     return {"achieved": achieved, "peak": peak, "unit": "Tinst/s (thread instructions)",
-            "frac": achieved / peak, "inst_per_update": NCU_INST_PER_UPDATE,
-            "inst_source": "ncu capture of the same workload"}
+            "frac": achieved / peak, "inst_per_update": ipu,
+            "inst_source": prof["source"], "stale": prof.get("stale", True)}
 
 
 def measured_peaks():
@@ -340,10 +368,17 @@ def run_ours(args, rank, world, local):
         peak = pk.value
     fused_share = (kms[0] + kms[1]) / kms[2]
     launches = s.launches_per_sweep() * args.steps
+    prof = profile_inputs()
 
     if rank != 0:
         s.close()
         return
+    s.close()
+    batched = map_err = None
+    if world == 1 and not args.no_batched:
+        batched = measure_batched(local)
+    if world == 1 and not args.no_map_error:
+        map_err = measure_map_error(local)
     cpu = None
     if world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -372,21 +407,102 @@ def run_ours(args, rank, world, local):
             "achieved": achieved_tflops, "peak": peak, "unit": "TFLOP/s",
             "frac": (achieved_tflops / peak) if peak else None,
             "peak_source": "measured FP32 FMA microbenchmark (bsg_fp32_peak)",
-            "traffic": NCU_TRAFFIC_PER_LAUNCH,
+            "traffic": prof.get("dram_bytes_per_launch"),
             "traffic_unit": "bytes per colour launch (ncu capture)",
+            "traffic_source": prof["source"], "stale": prof.get("stale", True),
             "algorithmic_bytes_per_launch": sweep_bytes(N, V, P, S) / 2,
             "flops_per_update": fused_flops_per_update(P),
             "fused_avg_launch_ms": fused_avg_ms, "fused_share_of_sweep": fused_share,
             "hbm_bytes_per_sweep": sweep_bytes(N, V, P, S),
             "hbm_achieved_gbs": sweep_bytes(N, V, P, S) / (ms_per_step * 1e-3) / 1e9,
             "hbm_peak_gbs": peaks.get("hbm_gbs"),
-            "issue": issue_roofline(local, N * V / 2 / (fused_avg_ms * 1e-3)),
+            "issue": issue_roofline(local, N * V / 2 / (fused_avg_ms * 1e-3), prof),
         },
         "cpu_baseline": cpu,
         "clocks": clocks,
+        "batched": batched,
+        "map_error": map_err,
     }
     print(json.dumps(line))
-    s.close()
+
+
+# ------------------------------------- headline: batched against plain ---
+BATCH_SEGMENT = {"c4": 32, "c3": 100, "c0": 100}  # sweeps per timed segment
+BATCH_MIN_MS = 1000.0  # device time of each batched measurement, at least
+
+
+def _segments(smp, T: int, min_ms: float) -> float:
+    """Device time per sweep of `smp` over graph segments of T sweeps
+    (CUDA events on its stream), repeated until at least min_ms."""
+    smp.run(T)  # instantiates the segment graphs
+    total, n = 0.0, 0
+    while total < min_ms or n < 2:
+        total += smp.run_timed(T)
+        n += 1
+    smp.sync()
+    return total / (n * T)
+
+
+def batched_vs_plain(name: str, local: int) -> dict:
+    """One workload of the headline metric: every chain / study in one
+    context (one launch per colour and P group, P groups on parallel graph
+    branches) against the plain single-chain form: each chain or study
+    alone in its own context, advanced by bsg_run graph segments of the same
+    length with no host synchronisation inside a segment (what a user of
+    one chain runs), one after another.  Device time per sweep; inputs and
+    state (hundreds of MB) exceed L2."""
+    import bsglmm_gb300 as bsg
+    studies, nchains = batched_workload(name)
+    T = BATCH_SEGMENT[name]
+    upd = sum(st.N * st.V * c for st, c in zip(studies, nchains))
+    with bsg.Sampler(local) as b:
+        for k, (st, nc) in enumerate(zip(studies, nchains)):
+            ds = b.add_dataset(st.mask, st.covar, st.data, st.nsubtypes)
+            for c in range(nc):
+                b.add_chain(ds, seed=1000 * k + c + 1)
+        with Clocks(local) as clk:
+            t_b = _segments(b, T, BATCH_MIN_MS)
+        launches = b.launches_per_sweep()
+    # plain: a lone chain of each study; identical chains of one study cost
+    # the same, so a study's nc chains take nc times its lone chain's time
+    t_p = 0.0
+    for k, (st, nc) in enumerate(zip(studies, nchains)):
+        with bsg.Sampler(local) as p:
+            ds = p.add_dataset(st.mask, st.covar, st.data, st.nsubtypes)
+            p.add_chain(ds, seed=1000 * k + 1)
+            t_p += nc * _segments(p, T, 200.0 / len(studies))
+    return {"workload": BATCHED[name], "chains": sum(nchains), "studies": len(studies),
+            "updates_per_sweep": upd, "segment_sweeps": T,
+            "batched": {"value": upd / (t_b * 1e-3), "ms_per_sweep": t_b,
+                        "launches_per_sweep": launches},
+            "plain": {"value": upd / (t_p * 1e-3), "ms_per_sweep": t_p,
+                      "form": "each chain alone in its own context, bsg_run segments"},
+            "batched_over_plain": t_p / t_b, "unit": UNIT, "timing": "device, CUDA events",
+            "clocks": clk.summary()}
+
+
+def measure_batched(local: int) -> dict:
+    out = {k: batched_vs_plain(k, local) for k in ("c4", "c3", "c0")}
+    out["meets_3x"] = {k: out[k]["batched_over_plain"] >= 3.0 for k in ("c4", "c3", "c0")}
+    return out
+
+
+MAP_ERROR_FILE = ROOT / "tests" / "golden" / "map_error_fp64.json"
+
+
+def measure_map_error(local: int) -> dict:
+    """The FP32 maps' error against the FP64 GPU chain, live on the
+    CPU-runnable study (20^3 sphere, N = 50, P = 3: 1000 burn-in + 20 x 100
+    kept sweeps, batch-means MCSE), plus the committed results of the
+    brain-sized studies (tests/golden/map_error_fp64.json)."""
+    from bsglmm_gb300 import precision, synth
+    live = precision.map_error_vs_fp64(synth.config0(0), seed=1, burnin=1000,
+                                       batches=20, batch=100, device=local)
+    out = {"c0_live": live}
+    if MAP_ERROR_FILE.exists():
+        out["committed"] = json.loads(MAP_ERROR_FILE.read_text())
+        out["committed_source"] = str(MAP_ERROR_FILE.relative_to(ROOT))
+    return out
 
 
 # ------------------------------------------------- batched workloads ---
@@ -652,6 +768,8 @@ def main():
     ap.add_argument("--lpv", type=int, default=0)
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-map-error", action="store_true")
     ap.add_argument("--workload", default="brain",
                     choices=["brain", "dic"] + sorted(VARIANTS) + sorted(BATCHED))
     args = ap.parse_args()

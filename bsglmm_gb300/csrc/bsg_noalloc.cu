@@ -292,8 +292,8 @@ cudaError_t scratch_for_current_device(unsigned long long **out) {
     g_ctx_tried = true;
     void *fn = nullptr;
     cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPoint("cuCtxGetCurrent", &fn, cudaEnableDefault, &q) ==
-            cudaSuccess &&
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
       g_ctx_get = reinterpret_cast<CtxGetCurrentFn>(fn);
   }

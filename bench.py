@@ -253,6 +253,7 @@ def run_reference(args, rank, world):
     per_step = min(10.0, max(0.25, CPU_REFERENCE_S / max(args.steps, 1)))
     rate, sec_per_step, sample = cpu_port_rate(study, threads, args.steps,
                                                args.warmup, per_step)
+    ref_gpu = reference_gpu_timing() if args.gpus >= 1 else None
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -265,8 +266,39 @@ def run_reference(args, rank, world):
                          "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "reference_gpu": ref_gpu,
     }
     print(json.dumps(line))
+
+
+REFGPU_TIMEOUT_S = 240
+
+
+def reference_gpu_timing() -> dict:
+    """The reference's own GPU form on this GPU (its covarGPU.cu kernels,
+    compiled to PTX from its source tree and driven as its launchers do,
+    oracle/refgpu_run.py), in a child process under a time limit: the
+    brain-sized study (2 warm-up + 10 timed sweeps) and the 20^3 study (20 +
+    200).  Each entry is that run's JSON line, or why it is missing."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    if not oracle.refgpu_available():
+        return {"unavailable": "oracle/_ref/covarGPU.ptx was not built (the reference "
+                               "tree was not mounted where the repository was built)"}
+    out = {"form": "the reference's covarGPU.cu kernels (PTX JIT-compiled for this GPU), "
+                   "driven as mcmc.cpp:314-394 drives them; host Wishart",
+           "timing": "CUDA events around whole sweeps (host-synchronous launchers)"}
+    for name, warm, timed in (("c1", 2, 10), ("c0", 20, 200)):
+        try:
+            r = subprocess.run([sys.executable, str(ROOT / "oracle" / "refgpu_run.py"), name,
+                                str(warm), str(timed)], capture_output=True, text=True,
+                               timeout=REFGPU_TIMEOUT_S)
+            last = r.stdout.strip().splitlines()[-1] if r.stdout.strip() else ""
+            out[name] = (json.loads(last) if r.returncode == 0 and last else
+                         {"unavailable": f"exit {r.returncode}: {r.stderr.strip()[-300:]}"})
+        except subprocess.TimeoutExpired:
+            out[name] = {"unavailable": f"timed out after {REFGPU_TIMEOUT_S} s"}
+    return out
 
 
 def flush_l2(buf):

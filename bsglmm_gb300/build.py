@@ -73,6 +73,26 @@ def _compile(src: str, force: bool, extra: list[str]) -> Path:
     return obj
 
 
+DRIVER_SRC = CSRC / "driver" / "bsglmm_main.cpp"
+DRIVER = OUT / "bsglmm"
+
+
+def build_driver(force: bool = False) -> Path:
+    """The `bsglmm` command (C++ driver over the C ABI), linked against the
+    in-tree library with an $ORIGIN run path."""
+    lib = lib_path()
+    hdr = PKG.parent / "include" / "bsglmm_gb300.h"
+    if (force or not DRIVER.exists()
+            or any(p.stat().st_mtime > DRIVER.stat().st_mtime for p in (DRIVER_SRC, hdr, lib))):
+        cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+        cmd = [cxx, "-O2", "-std=c++17", "-o", str(DRIVER), str(DRIVER_SRC), f"-L{OUT}",
+               "-lbsglmm_gb300", "-Wl,-rpath,$ORIGIN", "-ldl"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver build failed:\n{r.stderr}")
+    return DRIVER
+
+
 def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     OUT.mkdir(exist_ok=True)
@@ -85,6 +105,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
+    build_driver(force)
     return lib
 
 

@@ -485,3 +485,64 @@ class RefKiss(_Ref):
         out = np.zeros(n)
         self._L.ref_rgamma_many(a, b, n, _p(out))
         return out
+
+
+# ------------------------------------------- the reference's GPU sweep ---
+LIBREFGPU = HERE / "librefgpu.so"
+REF_PTX = HERE / "_ref" / "covarGPU.ptx"
+
+
+def refgpu_available() -> bool:
+    """The reference's covarGPU.cu compiled to PTX (made where the
+    reference tree is mounted; the file travels with the repository copy)
+    and the host harness that drives it."""
+    return REF_PTX.exists() and LIBREFGPU.exists()
+
+
+class RefGpu:
+    """The reference's own GPU kernels (Z_GPU1, Spat_Coef_Probit, reduce,
+    Spat_Coef_Prec from covarGPU.cu, JIT-loaded from PTX) driven as its
+    launchers do (refgpu_harness.cu).  One study per process."""
+
+    def __init__(self, pb: Problem, device: int = 0, seed: int = 1):
+        L = C.CDLL(str(LIBREFGPU))
+        L.rg_error.restype = C.c_char_p
+        L.rg_open.argtypes = [C.c_char_p, _i]
+        L.rg_setup.argtypes = [_i, _i, _i, _i, _i, _i, _i, _P, _P, _i, _P, _P, _i, _P,
+                               _P, _P, _P, _P, C.c_uint64]
+        L.rg_sweeps.argtypes = [_i, _P]
+        L.rg_get_beta.argtypes = [_P]
+        L.rg_get_omega.argtypes = [_P]
+        self._L = L
+        self.pb = pb
+        if L.rg_open(str(REF_PTX).encode(), device):
+            raise RuntimeError(L.rg_error().decode())
+        lat = pb.lattice()
+        self._keep = [np.ascontiguousarray(a) for a in (
+            lat["idx"], lat["idxsc"], lat["vox"][0], lat["nbrs"][0], lat["vox"][1],
+            lat["nbrs"][1], pb.covar, pb.data, pb.xtx())]
+        k = self._keep
+        if L.rg_setup(pb.X, pb.Y, pb.Z, pb.N, pb.P, pb.V, pb.Vp, _p(k[0]), _p(k[1]),
+                      pb.n0, _p(k[2]), _p(k[3]), pb.n1, _p(k[4]), _p(k[5]), _p(k[6]),
+                      _p(k[7]), _p(k[8]), seed):
+            raise RuntimeError(L.rg_error().decode())
+
+    def sweeps(self, n: int) -> float:
+        """Runs n sweeps; returns milliseconds per sweep."""
+        ms = C.c_double()
+        if self._L.rg_sweeps(n, C.byref(ms)):
+            raise RuntimeError(self._L.rg_error().decode())
+        return ms.value
+
+    def beta(self) -> np.ndarray:
+        out = np.zeros((self.pb.P, self.pb.Vp), np.float32)
+        self._L.rg_get_beta(_p(out))
+        return out
+
+    def omega(self) -> np.ndarray:
+        out = np.zeros((self.pb.P, self.pb.P), np.float32)
+        self._L.rg_get_omega(_p(out))
+        return out
+
+    def close(self):
+        self._L.rg_close()

@@ -511,6 +511,7 @@ class RefGpu:
         L.rg_setup.argtypes = [_i, _i, _i, _i, _i, _i, _i, _P, _P, _i, _P, _P, _i, _P,
                                _P, _P, _P, _P, C.c_uint64]
         L.rg_sweeps.argtypes = [_i, _P]
+        L.rg_set_model.argtypes = [_i]
         L.rg_get_beta.argtypes = [_P]
         L.rg_get_omega.argtypes = [_P]
         self._L = L
@@ -526,6 +527,11 @@ class RefGpu:
                       pb.n0, _p(k[2]), _p(k[3]), pb.n1, _p(k[4]), _p(k[5]), _p(k[6]),
                       _p(k[7]), _p(k[8]), seed):
             raise RuntimeError(L.rg_error().decode())
+
+    def set_model(self, model: int):
+        """The reference's MODEL: 1 probit, 0 logistic, 2 t."""
+        if self._L.rg_set_model(int(model)):
+            raise RuntimeError(self._L.rg_error().decode())
 
     def sweeps(self, n: int) -> float:
         """Runs n sweeps; returns milliseconds per sweep."""

@@ -16,7 +16,9 @@
 // copy, and the Wishart draw on the host.  The host Wishart here is this
 // file's own FP64 Bartlett draw (chol -> invert -> chol of S + I, df =
 // V + 19 as covarGPU.cu:1104), not the reference's randgen.cpp; it costs
-// microseconds at P <= 8.
+// microseconds at P <= 8.  With rg_set_model(0 or 2) it runs the t/logit
+// links instead: Z_GPU2 and Phi_GPU per colour, then the weighted
+// Spat_Coef (the MODEL != 1 branches of the same launchers).
 //
 // Only bench.py's reference arm and tests load this library (through
 // oracle.py); the product never does.
@@ -36,6 +38,12 @@ struct RefGpu {
   cudaLibrary_t lib = nullptr;
   cudaKernel_t k_setup = nullptr, k_z = nullptr, k_beta = nullptr, k_reduce = nullptr,
                k_prec = nullptr;
+  // the t/logit links (MODEL 0 and 2): Z_GPU2, Phi_GPU and the weighted
+  // Spat_Coef (covarGPU.cu:398-513,1430-1563)
+  cudaKernel_t k_z2 = nullptr, k_phi = nullptr, k_beta_w = nullptr;
+  int model = 1;
+  float t_df = 1000.f;
+  float *dphi = nullptr;
   void *d_prec_sym = nullptr, *d_xtx_sym = nullptr;
   // study
   int N = 0, P = 0, V = 0, Vp = 0, X = 0, Y = 0, n[2] = {0, 0};
@@ -136,8 +144,30 @@ int sweep() {
   const int P = g.P, nrow = g.X, ncol = g.Y, ncovfix = 0, nsubtypes = 1;
   const float beta_wm = 0.f, sqrt2 = std::sqrt(2.f);
   void *nullp = nullptr;
-  // updateZGPU (covarGPU.cu:1625-1669): Z_GPU1 per colour
-  for (int c = 0; c < 2; ++c) {
+  // updateZGPU (covarGPU.cu:1625-1669): Z_GPU2 (t/logit links) or Z_GPU1
+  // per colour; then updatePhiGPU (covarGPU.cu:1590-1612): Phi_GPU
+  if (g.model != 1) {
+    const float alp = (g.t_df + 1.f) / 2.f, df = g.t_df;
+    for (int pass = 0; pass < 2; ++pass)
+      for (int c = 0; c < 2; ++c) {
+        const int tpb = 96, nb = (g.n[c] + tpb - 1) / tpb;
+        if (nb == 0) continue;
+        int N = g.N, NC = g.n[c], Vp = g.Vp, V = g.V;
+        void *a_z[] = {&g.dZ,  &g.ddata, &g.dcovar, &nullp,  &nullp, &nullp, &g.dwm,
+                       &g.dbeta, (void *)&beta_wm, &g.dvox[c], &N, (void *)&nsubtypes,
+                       (void *)&P, (void *)&ncovfix, &NC, &Vp, &V, &g.dstates, &g.didx,
+                       &g.didxsc, (void *)&sqrt2, &g.dphi, &nullp, (void *)&alp,
+                       (void *)&df};
+        void *a_phi[] = {&g.dZ,  &g.ddata, &g.dcovar, &nullp,  &nullp, &nullp, &g.dwm,
+                         &g.dbeta, (void *)&beta_wm, &g.dvox[c], &N, (void *)&nsubtypes,
+                         (void *)&P, (void *)&ncovfix, &NC, &Vp, &V, &g.dstates, &g.didx,
+                         &g.didxsc, (void *)&sqrt2, &g.dphi, (void *)&alp, (void *)&df};
+        RG_CK(cudaLaunchKernel((const void *)(pass == 0 ? g.k_z2 : g.k_phi), dim3(nb),
+                               dim3(tpb), pass == 0 ? a_z : a_phi, sizeof(float) * P * tpb,
+                               0));
+      }
+  }
+  for (int c = 0; c < 2 && g.model == 1; ++c) {
     const int tpb = 96, nb = (g.n[c] + tpb - 1) / tpb;
     if (nb == 0) continue;
     int N = g.N, NC = g.n[c], Vp = g.Vp, V = g.V;
@@ -161,8 +191,14 @@ int sweep() {
                     &g.dbeta,  (void *)&beta_wm, &g.dnbrs[c], &g.dvox[c], &N, &X, &Y,
                     (void *)&nsubtypes, (void *)&P, (void *)&ncovfix, &NC, &Vp, &V,
                     &g.dstates, &g.didx, &g.didxsc};
-    RG_CK(cudaLaunchKernel((const void *)g.k_beta, dim3(nb), dim3(tpb), args,
-                           sizeof(float) * P * tpb, 0));
+    // the weighted update takes Phi after Z (covarGPU.cu:398)
+    void *args_w[] = {&g.dcovar, &nullp,  &nullp,  &nullp,    &g.dZ,   &g.dphi, &g.dwm,
+                      &g.dbeta,  (void *)&beta_wm, &g.dnbrs[c], &g.dvox[c], &N, &X, &Y,
+                      (void *)&nsubtypes, (void *)&P, (void *)&ncovfix, &NC, &Vp, &V,
+                      &g.dstates, &g.didx, &g.didxsc};
+    RG_CK(cudaLaunchKernel((const void *)(g.model == 1 ? g.k_beta : g.k_beta_w), dim3(nb),
+                           dim3(tpb), g.model == 1 ? args : args_w, sizeof(float) * P * tpb,
+                           0));
   }
   const int BPG = 32;
   for (int p = 0; p < P; ++p) {  // column means, one allocation each
@@ -229,7 +265,10 @@ int rg_open(const char *ptx_path, int device) {
               {"6Z_GPU1", &g.k_z},
               {"16Spat_Coef_Probit", &g.k_beta},
               {"6reduce", &g.k_reduce},
-              {"14Spat_Coef_Prec", &g.k_prec}};
+              {"14Spat_Coef_Prec", &g.k_prec},
+              {"6Z_GPU2", &g.k_z2},
+              {"7Phi_GPU", &g.k_phi},
+              {"9Spat_Coef", &g.k_beta_w}};
   std::string names;
   for (cudaKernel_t k : ks) {
     const char *name = nullptr;
@@ -292,6 +331,28 @@ int rg_setup(int X, int Y, int Z, int N, int P, int V, int Vp, const int32_t *id
   return 0;
 }
 
+// The link, the reference's compile-time MODEL (main.cu:42,168-175): 1
+// probit; 0 logistic (t_8 mixture) and 2 t (t_3), with the scale-mixture
+// weights Phi (N V floats) allocated here and set to 1, the value of the
+// reference's restart code (mcmc.cpp:1245): its own allocation of devicePhi
+// is commented out (mcmc.cpp:179-180), so this path cannot run as shipped.
+// The weighted Spat_Coef stages the design only from threads with a voxel,
+// so every colour must fill whole 192-voxel blocks (the caller's study
+// guarantees it; rg_set_model refuses otherwise).
+int rg_set_model(int model) {
+  if (model < 0 || model > 2) return fail("model must be 0, 1 or 2");
+  if (model != 1 && (g.n[0] % 192 || g.n[1] % 192))
+    return fail("the t/logit kernels need colour sizes that are multiples of 192");
+  g.model = model;
+  g.t_df = model == 0 ? 8.f : (model == 2 ? 3.f : 1000.f);
+  if (model != 1 && !g.dphi) {
+    const size_t n = (size_t)g.N * g.V;
+    std::vector<float> ones(n, 1.f);
+    if (upload(&g.dphi, ones.data(), n)) return 1;
+  }
+  return 0;
+}
+
 // Runs n sweeps; *ms = host wall time per sweep (the reference's loop is
 // host-synchronous: every launcher ends in a blocking copy).
 int rg_sweeps(int n, double *ms) {
@@ -334,6 +395,7 @@ void rg_close() {
   }
   cudaFree(g.didx);
   cudaFree(g.didxsc);
+  cudaFree(g.dphi);
   cudaFree(g.dstates);
   if (g.lib) cudaLibraryUnload(g.lib);
   g = RefGpu();

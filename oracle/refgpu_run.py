@@ -5,9 +5,13 @@ synthetic study, and prints one JSON line.  Run as a child process (bench.py's
 reference arm and the tests do, under a time limit):
 
     python oracle/refgpu_run.py <study> <warmup sweeps> <timed sweeps> [seed]
+    python oracle/refgpu_run.py chain <model> <burn-in> <kept sweeps> [seed]
 
 study: c0 (20^3 sphere, N = 50, P = 3) or c1 (91x109x91 ellipsoid,
-N = 1000, P = 5).  Inputs are finite and the chain starts from beta = 0,
+N = 1000, P = 5).  The chain form runs the box study (BOX below: both
+colours fill whole 192-voxel blocks, which the reference's weighted
+Spat_Coef needs) with the link `model` (1 probit, 0 logistic, 2 t) and
+prints, per kept sweep, the mean over the mask of every coefficient map.  Inputs are finite and the chain starts from beta = 0,
 Omega = I (mcmc.cpp:149-154,227), so the reference's unbounded rejection
 loops (covarGPU.cu:1126-1143,1170-1194) see finite means only.
 """
@@ -30,7 +34,35 @@ from bsglmm_gb300 import synth  # noqa: E402
 STUDIES = {"c0": lambda: synth.config0(0), "c1": lambda: synth.config1(seed=1)}
 
 
+def box_study():
+    """24 x 16 x 12 box (4,608 voxels, 2,304 per colour), N = 60, P = 3."""
+    mask = np.ones((12, 16, 24), np.uint8)
+    return synth.make_study("box", mask, 60, 3, 3.0, 0.2, 17)
+
+
+def chain(argv):
+    model, burn, kept = int(argv[0]), int(argv[1]), int(argv[2])
+    seed = int(argv[3]) if len(argv) > 3 else 1
+    st = box_study()
+    pb = oracle.Problem(st.mask, st.covar, st.data, st.nsubtypes)
+    rg = oracle.RefGpu(pb, seed=seed)
+    rg.set_model(model)
+    lat = pb.lattice()
+    cols = lat["idxsc"][lat["idx"] >= 0]
+    rg.sweeps(burn)
+    series = []
+    for _ in range(kept):
+        rg.sweeps(1)
+        series.append([float(x) for x in rg.beta()[:, cols].mean(axis=1)])
+    rg.close()
+    print(json.dumps({"model": model, "burnin": burn, "kept": kept, "V": int(st.V),
+                      "series": series}))
+
+
 def main(argv):
+    if argv[0] == "chain":
+        chain(argv[1:])
+        return
     name, warm, timed = argv[0], int(argv[1]), int(argv[2])
     seed = int(argv[3]) if len(argv) > 3 else 1
     st = STUDIES[name]()

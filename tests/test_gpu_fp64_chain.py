@@ -126,3 +126,19 @@ def test_fp64_mode_rejects_other_links_and_supplied_sweeps():
                              np.full(P, 10.0), np.zeros(P * (P - 1) // 2), form=1)
         s.set_precision(ch, 32)
         s.run(1)
+
+
+def test_map_error_study_on_a_small_study():
+    """bsglmm_gb300.precision.map_error_vs_fp64 end to end on a small study:
+    the FP32 chain on the FP64 chain's counters stays far inside 0.5 MCSE,
+    and the independent chain's z-scores look like Monte-Carlo noise."""
+    from bsglmm_gb300 import precision
+    name, st = _studies()[1]
+    r = precision.map_error_vs_fp64(st, seed=4, burnin=50, batches=10, batch=20)
+    print(r["beta"], r["prb"])
+    assert r["sweeps"] == 250 and r["P"] == st.P
+    for what in ("beta", "prb"):
+        assert r[what]["same_counters"]["max"] < 0.01
+        assert r[what]["same_counters"]["frac_le_0.5"] == 1.0
+        z = r[what]["independent_chain_z"]
+        assert 0.2 < z["median"] < 2.0 and z["frac_within_4"] > 0.97

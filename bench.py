@@ -406,9 +406,11 @@ def run_ours(args, rank, world, local):
         s.close()
         return
     s.close()
-    batched = map_err = None
+    batched = map_err = txz = None
     if world == 1 and not args.no_batched:
         batched = measure_batched(local)
+    if world == 1 and not args.no_tensor_xz:
+        txz = measure_tensor_xz(local, study)
     if world == 1 and not args.no_map_error:
         map_err = measure_map_error(local)
     cpu = None
@@ -454,6 +456,7 @@ def run_ours(args, rank, world, local):
         "clocks": clocks,
         "batched": batched,
         "map_error": map_err,
+        "tensor_xz": txz,
     }
     print(json.dumps(line))
 
@@ -516,6 +519,34 @@ def batched_vs_plain(name: str, local: int) -> dict:
 def measure_batched(local: int) -> dict:
     out = {k: batched_vs_plain(k, local) for k in ("c4", "c3", "c0")}
     out["meets_3x"] = {k: out[k]["batched_over_plain"] >= 3.0 for k in ("c4", "c3", "c0")}
+    return out
+
+
+def measure_tensor_xz(local: int, brain) -> dict:
+    """The A/B of the probit colour kernel's X'Z contraction: f32x2 FMAs
+    (SIMT, the default) against the tensor cores (BF16x3 split product,
+    bsg_set_tensor_xz), on the brain-sized study (N = 1000, P = 5) and the
+    precision study (N = 2000, P = 8): device time per colour launch
+    (CUDA events around plain launches) and per sweep (64-sweep segments,
+    at least 0.5 s), same chain and variates."""
+    import bsglmm_gb300 as bsg
+    from bsglmm_gb300 import synth
+    out = {"form": "mma.sync m16n8k16 BF16x3 (x_hi z_hi + x_hi z_lo + x_lo z_hi), "
+                   "FP32 accumulation, one warp per 32 voxels"}
+    for name, st in (("c1", brain), ("c2", synth.config2())):
+        res = {"N": st.N, "P": st.P, "V": st.V}
+        for mode, tc in (("simt", False), ("tensor", True)):
+            with bsg.Sampler(local) as s:
+                ds = s.add_dataset(st.mask, st.covar, st.data, st.nsubtypes)
+                s.add_chain(ds, seed=7)
+                s.set_tensor_xz(tc)
+                s.run(2)
+                kms, kl = s.profile(10)
+                t = _segments(s, 64, 500.0)
+            res[mode] = {"colour_ms": [kms[0] / kl[0], kms[1] / kl[1]], "ms_per_sweep": t,
+                         "value": st.N * st.V / (t * 1e-3)}
+        res["tensor_over_simt"] = res["simt"]["ms_per_sweep"] / res["tensor"]["ms_per_sweep"]
+        out[name] = res
     return out
 
 
@@ -802,6 +833,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-map-error", action="store_true")
+    ap.add_argument("--no-tensor-xz", action="store_true")
     ap.add_argument("--workload", default="brain",
                     choices=["brain", "dic"] + sorted(VARIANTS) + sorted(BATCHED))
     args = ap.parse_args()

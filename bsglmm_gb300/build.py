@@ -30,6 +30,7 @@ SOURCES = [
     "bsg_fused_mix.cu",
     "bsg_fused_wm.cu",
     "bsg_fp64.cu",
+    "bsg_fused_tc.cu",
     "bsg_kernels.cu",
     "bsg_peak.cu",
     "bsg_noalloc.cu",
@@ -37,7 +38,7 @@ SOURCES = [
     "bsg_api.cpp",
 ]
 HEADERS = ["bsg_device.cuh", "bsg_fused.cuh", "bsg_internal.h", "bsg_math.cuh",
-           "bsg_wishart.cuh"]
+           "bsg_wishart.cuh", "bsg_mma.cuh"]
 
 
 def nvcc() -> str:

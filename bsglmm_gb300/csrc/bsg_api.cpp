@@ -100,6 +100,7 @@ struct bsg_ctx {
   std::vector<Group> groups;
   int *any_status = nullptr;  // device word: OR of every chain's error bits
   int lpv = 1, threads = 256;
+  bool tc = false;  // probit X'Z on the tensor cores (BF16x3 split)
 #ifdef BSG_NO_PDL
   bool pdl = false;
 #else
@@ -409,6 +410,9 @@ cudaError_t launch_colour(bsg_ctx *ctx, const Group &g, int c, cudaStream_t st, 
                             (int)g.map[c].size(), c, st, pdl);
   if (g.wm_any)
     return launch_fused_wm(g.P, ctx->threads, ctx->d_ds, ctx->d_ch, g.d_map[c],
+                           (int)g.map[c].size(), c, st, pdl);
+  if (ctx->tc && ctx->lpv == 1)
+    return launch_fused_tc(g.P, ctx->threads, ctx->d_ds, ctx->d_ch, g.d_map[c],
                            (int)g.map[c].size(), c, st, pdl);
   const Supplied sup{};
   return launch_fused(g.P, ctx->lpv, ctx->threads, false, ctx->d_ds, ctx->d_ch,
@@ -883,6 +887,18 @@ bsg_status bsg_set_tuning(bsg_ctx *ctx, int32_t lanes_per_voxel,
     ctx->lpv = lpv;
     ctx->threads = thr;
     ctx->plan_valid = false;
+  }
+  return BSG_OK;
+}
+
+bsg_status bsg_set_tensor_xz(bsg_ctx *ctx, int32_t enable) {
+  if (!ctx) return BSG_ERR_INVALID;
+  const bool on = enable != 0;
+  if (on != ctx->tc) {
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    clear_graphs(ctx);  // the segments hold the other kernel
+    ctx->tc = on;
   }
   return BSG_OK;
 }

@@ -23,6 +23,7 @@
 
 #include <type_traits>
 
+#include "bsg_mma.cuh"
 #include "bsg_wishart.cuh"
 
 namespace bsg {
@@ -49,12 +50,16 @@ constexpr int fused_min_blocks() {
 // coefficient draw uses X' Phi X and X' Phi (Z - b_WM WM).
 // WMU: chains that draw beta_WM (one lane per voxel) also carry each voxel's
 // term of its conditional mean through the block partials.
-template <int P, int LPV, bool SUPP, bool MIX = false, bool WMU = false>
+// TC: the probit kernel's X'(Z - b_WM WM) on the tensor cores as a BF16x3
+// split product (bsg_mma.cuh), one lane per voxel; the rest is unchanged.
+template <int P, int LPV, bool SUPP, bool MIX = false, bool WMU = false, bool TC = false>
 __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
     fused_colour_kernel(const DatasetDev *__restrict__ dsv,
                         ChainDev *__restrict__ chv,
                         const BlockMap *__restrict__ map, int colour,
                         Supplied sup) {
+  static_assert(!TC || (!SUPP && !MIX && !WMU && LPV == 1),
+                "the tensor-core X'Z serves the probit production kernel");
   constexpr int NT = P * (P + 1) / 2;
   constexpr int PP = P <= 4 ? 4 : 8;  // design row padded to float4s
   // The probit kernel stages the design as subject pairs: pair row m holds
@@ -120,6 +125,20 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
   if (!SUPP) key.init(ch.key0, ch.key1);
   int ok = 1;
   const uint32_t *yb = d.ybits[colour];
+  // TC: the chunk's design slices and this warp's Z tile (dynamic shared
+  // memory), the warp's four 8-voxel accumulator tiles, and whether any lane
+  // of the warp has a voxel (the MMAs need the whole warp: lanes without one
+  // contribute zeros)
+  extern __shared__ __align__(16) unsigned char tc_smem[];
+  unsigned char *tc_zt = TC ? tc_smem + kTcSlices * kTcSliceBytesPerCov * P + 16 +
+                                  (tid >> 5) * kTcZTileBytes
+                            : nullptr;
+  float tcd[TC ? 4 : 1][4];
+#pragma unroll
+  for (int jt = 0; jt < (TC ? 4 : 1); ++jt)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) tcd[jt][q] = 0.f;
+  const bool run = TC ? __any_sync(0xffffffffu, active) : active;
 
   for (int i0 = 0; i0 < N; i0 += kChunk) {
     const int cn = min(kChunk, N - i0);
@@ -134,8 +153,9 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
         Xs[(ii + (ii >> 5)) * PP + p] = xv;
       }
     }
+    if constexpr (TC) tc_stage_design<P>(tc_smem, d.covar, N, i0, cn, tid, blockDim.x);
     __syncthreads();
-    if (active) {
+    if (run) {
       // One subject: mu = bwm + x'beta; a = -mu if Y = 1 else mu (sign-bit
       // flip by ymask = Y << 31); t ~ N(0,1) on (a, inf);
       // Z - bwm = x'beta + (Y ? t : -t); acc += x (Z - bwm).
@@ -284,18 +304,29 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
                 zh[q >> 1].x = z;
             }
         }
+        if constexpr (TC) {
+          // the eight values go to this voxel's row of the warp's Z tile
+          // (zeros from lanes without a voxel); the MMAs follow per slice
+          if constexpr (H == 4) {
+            float2 zz[4];
 #pragma unroll
-        for (int h = 0; h < H; ++h) {
-          const float *xr = xr0 + h * RW;
-#pragma unroll
-          for (int p = 0; p + 1 < P; p += 2) {
-            const float4 v4 = *reinterpret_cast<const float4 *>(xr + 2 * p);
-            acc2[p] = fma2(make_float2(v4.x, v4.y), zh[h], acc2[p]);
-            acc2[p + 1] = fma2(make_float2(v4.z, v4.w), zh[h], acc2[p + 1]);
+            for (int h = 0; h < 4; ++h) zz[h] = active ? zh[h] : make_float2(0.f, 0.f);
+            tc_store_z(tc_zt, tid & 31, (ii0 >> 3) & 1, zz);
           }
-          if (P & 1)
-            acc2[P - 1] = fma2(*reinterpret_cast<const float2 *>(xr + 2 * (P - 1)), zh[h],
-                               acc2[P - 1]);
+        } else {
+#pragma unroll
+          for (int h = 0; h < H; ++h) {
+            const float *xr = xr0 + h * RW;
+#pragma unroll
+            for (int p = 0; p + 1 < P; p += 2) {
+              const float4 v4 = *reinterpret_cast<const float4 *>(xr + 2 * p);
+              acc2[p] = fma2(make_float2(v4.x, v4.y), zh[h], acc2[p]);
+              acc2[p + 1] = fma2(make_float2(v4.z, v4.w), zh[h], acc2[p + 1]);
+            }
+            if (P & 1)
+              acc2[P - 1] = fma2(*reinterpret_cast<const float2 *>(xr + 2 * (P - 1)), zh[h],
+                                 acc2[P - 1]);
+          }
         }
       };
       // The t/logit links, four subjects: Z by inversion and the first
@@ -409,7 +440,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
       const int nw = (cn + 31) >> 5;
       for (int wl = k; wl < nw; wl += LPV) {
         const int w = (i0 >> 5) + wl;
-        uint32_t yw = __ldg(yb + (size_t)w * nc + j);
+        uint32_t yw = (TC && !active) ? 0u : __ldg(yb + (size_t)w * nc + j);
         const int nbits = min(32, cn - (wl << 5));
         const int xo = (wl << 5) + wl;  // padded offset of bit 0
         const uint32_t i00 = (uint32_t)(i0 + (wl << 5));
@@ -423,7 +454,9 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
         // group ahead (the stores of the current group may alias as far as
         // the compiler knows, so it would not hoist them itself)
         const float *phb = MIX ? ch.phi[colour] + j : nullptr;
-        if (nbits == 32) {
+        // (TC: a ragged last word also takes the whole-word path; its
+        // subjects beyond the chunk have x = 0 and add nothing)
+        if (TC || nbits == 32) {
           float phc[4] = {1.f, 1.f, 1.f, 1.f}, phx[4] = {1.f, 1.f, 1.f, 1.f};
           if (MIX) {
 #pragma unroll
@@ -438,6 +471,13 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
                   philox(make_uint4((i >> 2) + 1, (uint32_t)v, sweep, cid | kTagZ), key)};
               groupp(std::integral_constant<int, 2>{}, (wl << 5) + b, yw, rs, i);
               yw >>= 8;
+              if constexpr (TC) {
+                if (b & 8) {  // a 16-subject slice is complete
+                  __syncwarp();
+                  tc_slice<P>(tc_smem, ((wl << 5) + b) >> 4, tc_zt, tid & 31, tcd);
+                  __syncwarp();
+                }
+              }
             }
           } else {
 #pragma unroll 1
@@ -496,7 +536,9 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
     }
   }
 
-  if constexpr (PAIRX) {
+  if constexpr (TC) {
+    if (run) tc_finish<P>(tc_zt, tid & 31, tcd, acc);
+  } else if constexpr (PAIRX) {
 #pragma unroll
     for (int p = 0; p < P; ++p) acc[p] = acc2[p].x + acc2[p].y;
   }
@@ -829,7 +871,7 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
 // programmatic-stream-serialization attribute, so it may start once every
 // block of the previous kernel in the stream has passed its dependency
 // point.
-template <int P, int LPV, bool SUPP, bool MIX = false, bool WMU = false>
+template <int P, int LPV, bool SUPP, bool MIX = false, bool WMU = false, bool TC = false>
 cudaError_t launch_one(int nblocks, int threads, cudaStream_t st, bool pdl,
                        const DatasetDev *ds, ChainDev *ch, const BlockMap *map,
                        int colour, const Supplied &sup) {
@@ -837,13 +879,23 @@ cudaError_t launch_one(int nblocks, int threads, cudaStream_t st, bool pdl,
   cfg.gridDim = dim3(nblocks);
   cfg.blockDim = dim3(threads);
   cfg.dynamicSmemBytes = 0;
+  if constexpr (TC) {
+    // the design slices and Z tiles (beyond the default 48 KB with the
+    // static design staging), set once per instantiation
+    const int bytes = tc_smem_bytes(P, kMaxThreads);
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        fused_colour_kernel<P, LPV, SUPP, MIX, WMU, TC>,
+        cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (attr != cudaSuccess) return attr;
+    cfg.dynamicSmemBytes = (size_t)tc_smem_bytes(P, threads);
+  }
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = pdl ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, fused_colour_kernel<P, LPV, SUPP, MIX, WMU>, ds, ch,
+  return cudaLaunchKernelEx(&cfg, fused_colour_kernel<P, LPV, SUPP, MIX, WMU, TC>, ds, ch,
                             map, colour, sup);
 }
 

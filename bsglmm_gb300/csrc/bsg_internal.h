@@ -154,6 +154,11 @@ constexpr int kMixLpv = 2;
 cudaError_t launch_fused_mix(int P, int threads, const DatasetDev *ds, ChainDev *ch,
                              const BlockMap *map, int nblocks, int colour,
                              cudaStream_t st, bool pdl);
+// The probit colour kernel with X'Z on the tensor cores (BF16x3 split, one
+// lane per voxel, Philox), bsg_fused_tc.cu.
+cudaError_t launch_fused_tc(int P, int threads, const DatasetDev *ds, ChainDev *ch,
+                            const BlockMap *map, int nblocks, int colour, cudaStream_t st,
+                            bool pdl);
 // The colour kernel of FP64 chains (bsg_fp64.cu): one thread per voxel,
 // kF64Threads voxels per block, Philox variates, probit link.
 cudaError_t launch_fp64(int P, const DatasetDev *ds, ChainDev *ch, const BlockMap *map,

@@ -101,6 +101,12 @@ class Sampler:
         self._check(self._L.bsg_set_tuning(self._h, lanes_per_voxel,
                                            block_threads), "bsg_set_tuning")
 
+    def set_tensor_xz(self, enable: bool = True):
+        """X'Z of the probit colour kernel on the tensor cores (BF16x3
+        split product) instead of f32x2 FMAs."""
+        self._check(self._L.bsg_set_tensor_xz(self._h, int(bool(enable))),
+                    "bsg_set_tensor_xz")
+
     def tuning(self):
         a, b = C.c_int32(), C.c_int32()
         self._check(self._L.bsg_get_tuning(self._h, C.byref(a), C.byref(b)),

@@ -93,6 +93,16 @@ bsg_status bsg_set_tuning(bsg_ctx *ctx, int32_t lanes_per_voxel,
 bsg_status bsg_get_tuning(const bsg_ctx *ctx, int32_t *lanes_per_voxel,
                           int32_t *block_threads);
 
+/* X'(Z - beta_WM WM) of the probit colour kernel (the reference's loop at
+ * covarGPU.cu:327-351) on the tensor cores: a BF16x3 split product (x = hi +
+ * lo, z = hi + lo, x_hi z_hi + x_hi z_lo + x_lo z_hi) with m16n8k16 MMAs per
+ * warp, accumulated in FP32.  Off by default (the SIMT path: f32x2 FMAs);
+ * it applies to probit chains without the beta_WM update at one lane per
+ * voxel, the others keep their kernels.  The draws are the same; the
+ * contraction differs from the SIMT path by the split's rounding (about
+ * 2^-16 relative per product).  No counterpart in the reference. */
+bsg_status bsg_set_tensor_xz(bsg_ctx *ctx, int32_t enable);
+
 /* ------------------------------------------------------------ sampling -- */
 /* Advances every chain by nsweeps sweeps (one sweep = latent Z + beta for
  * both colours, the Omega Wishart draw, and on kept sweeps the posterior

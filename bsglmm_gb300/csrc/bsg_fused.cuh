@@ -883,10 +883,10 @@ cudaError_t launch_one(int nblocks, int threads, cudaStream_t st, bool pdl,
     // the design slices and Z tiles (beyond the default 48 KB with the
     // static design staging), set once per instantiation
     const int bytes = tc_smem_bytes(P, kMaxThreads);
-    static const cudaError_t attr = cudaFuncSetAttribute(
+    static const cudaError_t opted = cudaFuncSetAttribute(
         fused_colour_kernel<P, LPV, SUPP, MIX, WMU, TC>,
         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (attr != cudaSuccess) return attr;
+    if (opted != cudaSuccess) return opted;
     cfg.dynamicSmemBytes = (size_t)tc_smem_bytes(P, threads);
   }
   cfg.stream = st;

@@ -16,7 +16,9 @@
 // Outputs (FLOAT64 NIfTI-1, gzipped in process): empir_prb_<group>,
 // total_lesion_cnt, total_empir_prb, spatCoef_<cov>, spatCoef_<cov>.Var,
 // standCoef_<cov>, prb_<group>, bWM (with a WM image); Qhat.dat, Qhat2.dat
-// and DIC.dat from the predictive pass run after every kept sweep.
+// and DIC.dat from the predictive pass run after every kept sweep.  Every
+// segment of up to 100 sweeps also prints one JSON line on stderr: the
+// sweep range, device milliseconds per sweep and subject-voxel updates/s.
 //
 // The chain runs MaxIter+1 sweeps with the reference's burn-in and SAVE_ITER
 // thinning (mcmc.cpp:303-308) and the reference GPU path's Wishart df
@@ -85,11 +87,6 @@ struct Zlib {
 Zlib &zlib() {
   static Zlib z;
   return z;
-}
-
-bool file_exists(const std::string &p) {
-  std::ifstream f(p, std::ios::binary);
-  return f.good();
 }
 
 // The whole file, gunzipped when it starts with the gzip magic.
@@ -531,8 +528,15 @@ int run(int ntypes, int ncov, const std::string &design_path, const std::string 
       check(ctx, bsg_get_colmeans(ctx, ch, colmean.data()), "bsg_get_colmeans");
       print_state(done, omega, colmean, P, ntypes);
     }
-    check(ctx, bsg_run(ctx, step), "bsg_run");
+    double ms = 0.0;
+    check(ctx, bsg_run_timed(ctx, step, &ms), "bsg_run_timed");
     check(ctx, bsg_sync(ctx), "bsg_sync");
+    // one machine-readable line per segment on stderr
+    std::fprintf(stderr,
+                 "{\"sweeps\": [%d, %d], \"ms_per_sweep\": %.6g, "
+                 "\"updates_per_s\": %.6g, \"status\": 0}\n",
+                 done, done + step - 1, ms / step,
+                 (double)N * (double)V * step / (ms > 0 ? ms * 1e-3 : 1e-300));
     done += step;
   }
   std::vector<double> sc((size_t)P * R), var((size_t)P * R), st((size_t)P * R),

@@ -16,6 +16,8 @@ read_data.cpp:187-545, mcmc.cpp:795-964):
   NIfTI-1 image in ./images; WM_v = value / 255 (read_data.cpp:489-545) and
   the white-matter coefficient beta_WM is drawn every sweep.
 * seed.dat: three integers (KISS state); rewritten at exit.
+* Every segment of up to 100 sweeps prints one JSON line on stderr: the sweep
+  range, device milliseconds per sweep and subject-voxel updates/s.
 * Outputs (FLOAT64 NIfTI-1, gzipped in process): empir_prb_<group>,
   total_lesion_cnt, total_empir_prb, spatCoef_<cov>, spatCoef_<cov>.Var,
   standCoef_<cov>, prb_<group>; text: Qhat.dat, Qhat2.dat (mcmc.cpp:719-786)
@@ -28,6 +30,7 @@ covarGPU.cu:1104).  GPU = 1 only.
 """
 from __future__ import annotations
 
+import json
 import sys
 from pathlib import Path
 
@@ -257,7 +260,13 @@ def run(ntypes, ncov, design, mask_name, maxiter, burnin, outdir=Path("."),
             step = min(PRINT_EVERY, maxiter + 1 - done)
             if not quiet and done % PRINT_EVERY == 0:
                 _print_state(done, s.omega(ch), s.colmeans(ch), ntypes)
-            s.run(step)
+            ms = s.run_timed(step)
+            s.sync()
+            # one machine-readable line per segment on stderr
+            sys.stderr.write(json.dumps({
+                "sweeps": [done, done + step - 1], "ms_per_sweep": ms / step,
+                "updates_per_s": data.shape[0] * data.shape[1] * step / max(ms * 1e-3, 1e-300),
+                "status": 0}) + "\n")
             done += step
         maps = s.maps(ch)
         totsav = s.sweep_count(ch)[1]

@@ -128,6 +128,28 @@ def test_fp64_mode_rejects_other_links_and_supplied_sweeps():
         s.run(1)
 
 
+def test_fp64_chain_matches_cpu_oracle_on_the_brain_study(oracle_mod):
+    """The brain-sized study (230,261 voxels, N = 1000, P = 5), two sweeps
+    (the second with the first's Omega): the FP64 GPU chain equals the CPU
+    FP64 oracle chain to 1e-9."""
+    import bsglmm_gb300 as bsg
+    from bsglmm_gb300 import synth
+    st = synth.config1(seed=1)
+    pb = oracle_mod.Problem(st.mask, st.covar, st.data, st.nsubtypes)
+    o = pb.chain(0xB64, 2)
+    assert o["err"] == 0
+    with bsg.Sampler() as s:
+        ds = s.add_dataset(st.mask, st.covar, st.data, st.nsubtypes)
+        ch = s.add_chain(ds, seed=0xB64)
+        s.set_precision(ch, 64)
+        s.run(2)
+        b64, om = s.beta64(ch), s.omega(ch)
+    print(f"brain study, FP64 GPU vs CPU oracle: beta {np.abs(b64 - o['beta']).max():.3g}, "
+          f"Omega {np.abs(om - o['omega']).max():.3g}")
+    assert np.allclose(b64, o["beta"], rtol=TOL64, atol=TOL64)
+    assert np.allclose(om, o["omega"], rtol=TOL64, atol=TOL64)
+
+
 def test_map_error_study_on_a_small_study():
     """bsglmm_gb300.precision.map_error_vs_fp64 end to end on a small study:
     the FP32 chain on the FP64 chain's counters stays far inside 0.5 MCSE,

@@ -498,6 +498,10 @@ def batched_vs_plain(name: str, local: int) -> dict:
         with Clocks(local) as clk:
             t_b = _segments(b, T, BATCH_MIN_MS)
         launches = b.launches_per_sweep()
+        # the 16 chains of one study: Gelman-Rubin R-hat of every coefficient
+        # map entry across them (config 4's reported convergence measure)
+        rhat = (cross_chain_rhat(b, sum(nchains), RHAT_BURNIN, RHAT_SWEEPS)
+                if name == "c4" else None)
     # plain: a lone chain of each study; identical chains of one study cost
     # the same, so a study's nc chains take nc times its lone chain's time
     t_p = 0.0
@@ -513,7 +517,7 @@ def batched_vs_plain(name: str, local: int) -> dict:
             "plain": {"value": upd / (t_p * 1e-3), "ms_per_sweep": t_p,
                       "form": "each chain alone in its own context, bsg_run segments"},
             "batched_over_plain": t_p / t_b, "unit": UNIT, "timing": "device, CUDA events",
-            "clocks": clk.summary()}
+            "clocks": clk.summary(), "rhat": rhat}
 
 
 def measure_batched(local: int) -> dict:

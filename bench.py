@@ -499,7 +499,7 @@ def batched_vs_plain(name: str, local: int) -> dict:
             t_b = _segments(b, T, BATCH_MIN_MS)
         launches = b.launches_per_sweep()
         # the 16 chains of one study: Gelman-Rubin R-hat of every coefficient
-        # map entry across them (config 4's reported convergence measure)
+        # map entry across them (the convergence measure reported for it)
         rhat = (cross_chain_rhat(b, sum(nchains), RHAT_BURNIN, RHAT_SWEEPS)
                 if name == "c4" else None)
     # plain: a lone chain of each study; identical chains of one study cost

@@ -120,7 +120,7 @@ def make_study(name: str, mask: np.ndarray, N: int, P: int, fwhm: float,
     return Study(name, mask, X, data, beta, 1, names[:P])
 
 
-# --------------------------------------------------------------- configs --
+# ------------------------------------------------------- the benchmark studies --
 def config0(seed: int = 0) -> Study:
     """20^3 grid, sphere r = 9 about (10.5, 10.5, 10.5), N = 50, P = 3,
     FWHM 3, intercept Phi^-1(0.05)."""
@@ -139,14 +139,14 @@ def config1(seed: int = 1, N: int = 1000) -> Study:
 
 
 def config2(seed: int = 2) -> Study:
-    """The config-1 mask with N = 2000 and P = 8."""
+    """The brain-sized ellipsoid mask with N = 2000 and P = 8."""
     return make_study("c2", ellipsoid_mask(BRAIN_SHAPE, BRAIN_AXES), 2000, 8,
                       4.0, 0.03, seed, "brain")
 
 
 def config3(seed: int = 3, ndatasets: int = 64):
     """Replicate studies: cube side U{32..64}, sphere radius 60-90% of the
-    half side, N U{40..400}, P U{2..6}, config-0 recipe, per-study seeds."""
+    half side, N U{40..400}, P U{2..6}, the 20^3 study's recipe, per-study seeds."""
     rng = np.random.default_rng(seed)
     out = []
     for d in range(ndatasets):

@@ -897,6 +897,7 @@ bsg_status bsg_set_tensor_xz(bsg_ctx *ctx, int32_t enable) {
   if (on != ctx->tc) {
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (on) CK(prepare_fused_tc());
     clear_graphs(ctx);  // the segments hold the other kernel
     ctx->tc = on;
   }

@@ -879,16 +879,9 @@ cudaError_t launch_one(int nblocks, int threads, cudaStream_t st, bool pdl,
   cfg.gridDim = dim3(nblocks);
   cfg.blockDim = dim3(threads);
   cfg.dynamicSmemBytes = 0;
-  if constexpr (TC) {
-    // the design slices and Z tiles (beyond the default 48 KB with the
-    // static design staging), set once per instantiation
-    const int bytes = tc_smem_bytes(P, kMaxThreads);
-    static const cudaError_t opted = cudaFuncSetAttribute(
-        fused_colour_kernel<P, LPV, SUPP, MIX, WMU, TC>,
-        cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (opted != cudaSuccess) return opted;
-    cfg.dynamicSmemBytes = (size_t)tc_smem_bytes(P, threads);
-  }
+  // the design slices and Z tiles of the tensor-core X'Z (the opt-in above
+  // the default 48 KB is made by prepare_tc, outside any stream capture)
+  if constexpr (TC) cfg.dynamicSmemBytes = (size_t)tc_smem_bytes(P, threads);
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -897,6 +890,14 @@ cudaError_t launch_one(int nblocks, int threads, cudaStream_t st, bool pdl,
   cfg.numAttrs = pdl ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, fused_colour_kernel<P, LPV, SUPP, MIX, WMU, TC>, ds, ch,
                             map, colour, sup);
+}
+
+// The dynamic shared memory opt-in of one tensor-core instantiation.
+template <int P>
+cudaError_t prepare_tc() {
+  return cudaFuncSetAttribute(fused_colour_kernel<P, 1, false, false, false, true>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              tc_smem_bytes(P, kMaxThreads));
 }
 
 // Instantiation helper used by bsg_fused_l*.cu.

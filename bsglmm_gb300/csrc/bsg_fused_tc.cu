@@ -4,6 +4,17 @@
 #include "bsg_fused.cuh"
 
 namespace bsg {
+// The kernels' dynamic shared memory opt-in (the chunk's BF16 design slices
+// and the warps' Z tiles exceed the default 48 KB with the static staging).
+// Called on the host before any launch, outside stream capture.
+cudaError_t prepare_fused_tc() {
+  const cudaError_t e[8] = {prepare_tc<1>(), prepare_tc<2>(), prepare_tc<3>(), prepare_tc<4>(),
+                            prepare_tc<5>(), prepare_tc<6>(), prepare_tc<7>(), prepare_tc<8>()};
+  for (cudaError_t x : e)
+    if (x != cudaSuccess) return x;
+  return cudaSuccess;
+}
+
 cudaError_t launch_fused_tc(int P, int threads, const DatasetDev *ds, ChainDev *ch,
                             const BlockMap *map, int nblocks, int colour, cudaStream_t st,
                             bool pdl) {

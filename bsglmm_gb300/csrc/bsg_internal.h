@@ -159,6 +159,8 @@ cudaError_t launch_fused_mix(int P, int threads, const DatasetDev *ds, ChainDev 
 cudaError_t launch_fused_tc(int P, int threads, const DatasetDev *ds, ChainDev *ch,
                             const BlockMap *map, int nblocks, int colour, cudaStream_t st,
                             bool pdl);
+// Its dynamic shared memory opt-in, before the first launch on a device.
+cudaError_t prepare_fused_tc();
 // The colour kernel of FP64 chains (bsg_fp64.cu): one thread per voxel,
 // kF64Threads voxels per block, Philox variates, probit link.
 cudaError_t launch_fp64(int P, const DatasetDev *ds, ChainDev *ch, const BlockMap *map,

@@ -787,6 +787,8 @@ def run_variant(args, rank, world, local):
         with bsg.Sampler(local) as s:
             ds = s.add_dataset(study.mask, study.covar, study.data, S, wm)
             ch = s.add_chain(ds, seed=chain_seed(rank), burnin=0, thin=1)
+            if args.tensor_xz:
+                s.set_tensor_xz(True)
             setup(s, ch)
             for _ in range(args.warmup):
                 s.run_timed(1)
@@ -838,6 +840,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-map-error", action="store_true")
     ap.add_argument("--no-tensor-xz", action="store_true")
+    ap.add_argument("--tensor-xz", action="store_true",
+                    help="model-variant workloads: X'Z on the tensor cores")
     ap.add_argument("--workload", default="brain",
                     choices=["brain", "dic"] + sorted(VARIANTS) + sorted(BATCHED))
     args = ap.parse_args()

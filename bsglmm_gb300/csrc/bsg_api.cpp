@@ -1488,23 +1488,28 @@ bsg_status bsg_autotune(bsg_ctx *ctx, int32_t sweeps, int32_t *best_lpv,
   const int lpvs[] = {1, 2, 4, 8}, thrs[] = {64, 128, 256};
   double best = 1e300;
   int bl = ctx->lpv, bt = ctx->threads;
+  bool btc = ctx->tc;
   for (int lpv : lpvs)
-    for (int thr : thrs) {
-      if (thr / lpv < 8) continue;
-      bsg_status s = bsg_set_tuning(ctx, lpv, thr);
-      if (!s) s = bsg_run(ctx, 1);  // warm-up and graph capture
-      double ms = 0;
-      if (!s) s = bsg_run_timed(ctx, sweeps, &ms);
-      for (size_t i = 0; i < ctx->ch.size() && !s; ++i)
-        s = bsg_restore(ctx, (int32_t)i, saved[i].data(), (int64_t)saved[i].size());
-      if (s) return s;
-      if (ms < best) {
-        best = ms;
-        bl = lpv;
-        bt = thr;
+    for (int thr : thrs)
+      for (int tc = 0; tc < (lpv == 1 ? 2 : 1); ++tc) {  // X'Z: SIMT, tensor cores
+        if (thr / lpv < 8) continue;
+        bsg_status s = bsg_set_tuning(ctx, lpv, thr);
+        if (!s) s = bsg_set_tensor_xz(ctx, tc);
+        if (!s) s = bsg_run(ctx, 1);  // warm-up and graph capture
+        double ms = 0;
+        if (!s) s = bsg_run_timed(ctx, sweeps, &ms);
+        for (size_t i = 0; i < ctx->ch.size() && !s; ++i)
+          s = bsg_restore(ctx, (int32_t)i, saved[i].data(), (int64_t)saved[i].size());
+        if (s) return s;
+        if (ms < best) {
+          best = ms;
+          bl = lpv;
+          bt = thr;
+          btc = tc != 0;
+        }
       }
-    }
   bsg_status s = bsg_set_tuning(ctx, bl, bt);
+  if (!s) s = bsg_set_tensor_xz(ctx, btc ? 1 : 0);
   if (s) return s;
   if (best_lpv) *best_lpv = bl;
   if (best_threads) *best_threads = bt;

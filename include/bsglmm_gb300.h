@@ -229,9 +229,11 @@ int64_t bsg_checkpoint_size(const bsg_ctx *ctx, int32_t chain);
 bsg_status bsg_checkpoint(bsg_ctx *ctx, int32_t chain, void *buf, int64_t size);
 bsg_status bsg_restore(bsg_ctx *ctx, int32_t chain, const void *buf,
                        int64_t size);
-/* Times each supported tile shape (lanes per voxel x threads per block) on
- * the context's chains for `sweeps` sweeps, keeps the fastest and puts every
- * chain back to its state before the call. */
+/* Times each supported tile shape (lanes per voxel x threads per block,
+ * and at one lane per voxel both X'Z paths of bsg_set_tensor_xz) on the
+ * context's chains for `sweeps` sweeps, keeps the fastest (the X'Z path
+ * stays set on the context) and puts every chain back to its state before
+ * the call. */
 bsg_status bsg_autotune(bsg_ctx *ctx, int32_t sweeps, int32_t *lanes_per_voxel,
                         int32_t *block_threads);
 

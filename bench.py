@@ -54,7 +54,7 @@ CPU_REFERENCE_S = 90.0  # seconds of CPU work in a whole reference-arm run
 # changed since.
 PROFILE = ROOT / "profiles" / "fused_colour_kernel_brain_c1.md"
 KERNEL_SOURCES = ["bsg_fused.cuh", "bsg_device.cuh", "bsg_math.cuh", "bsg_wishart.cuh",
-                  "bsg_internal.h", "bsg_fused_l1.cu"]
+                  "bsg_internal.h", "bsg_fused_l1.cu", "bsg_mma.cuh"]
 
 
 def kernel_sources_hash() -> str:

@@ -30,7 +30,7 @@ OUT = Path(__file__).resolve().parent / "map_error_fp64.json"
 
 RUNS = {
     # study, seed, burnin, batches, batch
-    "c1": (lambda: synth.config1(seed=1), 11, 500, 20, 100),
+    "c1": (lambda: synth.config1(seed=1), 11, 500, 40, 200),
     "c2": (lambda: synth.config2(), 12, 300, 40, 200),
 }
 

@@ -5,8 +5,8 @@ N = 1000, P = 5 and with N = 2000, P = 8, every coefficient and
 lesion-probability map entry of the FP32 chain lies within 0.5 MCSE of the
 FP64 chain on the same counters (the headline's accuracy condition), and an
 independent FP32 chain agrees with the FP64 chain within 4 combined MCSE on
-at least 99.5 % of the entries (batch means over 20 batches, whose MCSE
-estimates carry t(19) tails)."""
+at least 99.5 % of the entries (batch means over 40 batches, whose MCSE
+estimates carry t(39) tails)."""
 from __future__ import annotations
 
 import json

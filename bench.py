@@ -44,6 +44,7 @@ UNIT = "subject-voxel updates/s"
 WORKLOAD = "brain-sized plain FP32 GPU form: 91x109x91 grid, ellipsoid mask, N=1000, P=5"
 C_TN = 40          # FP32 flops of one truncated-normal draw's accept path
 L2_FLUSH_BYTES = 512 << 20
+L2_MB = 129  # GB300 L2
 CPU_CAL_VOX = 2000      # voxels per colour of the CPU calibration sweep
 CPU_BASELINE_S = 10.0   # seconds of CPU work in the cpu_baseline sample
 CPU_REFERENCE_S = 90.0  # seconds of CPU work in a whole reference-arm run
@@ -478,18 +479,27 @@ def _segments(smp, T: int, min_ms: float) -> float:
     return total / (n * T)
 
 
-def batched_vs_plain(name: str, local: int) -> dict:
+def batched_vs_plain(name: str, local: int, rhat=(None, None)) -> dict:
     """One workload of the headline metric: every chain / study in one
     context (one launch per colour and P group, P groups on parallel graph
     branches) against the plain single-chain form: each chain or study
     alone in its own context, advanced by bsg_run graph segments of the same
     length with no host synchronisation inside a segment (what a user of
-    one chain runs), one after another.  Device time per sweep; inputs and
-    state (hundreds of MB) exceed L2."""
+    one chain runs), one after another.  Device time per sweep, with no L2
+    flush inside a segment: the line states each form's working set against
+    the 129 MB L2 (the 64-chain 20^3 study fits in it, so both forms run
+    L2-resident there, as a chain that small does in steady state).  `rhat`
+    = (burn-in, sweeps) of the c4 R-hat, None for the defaults."""
     import bsglmm_gb300 as bsg
     studies, nchains = batched_workload(name)
+    rh_burnin = RHAT_BURNIN if rhat[0] is None else rhat[0]
+    rh_sweeps = RHAT_SWEEPS if rhat[1] is None else rhat[1]
     T = BATCH_SEGMENT[name]
     upd = sum(st.N * st.V * c for st, c in zip(studies, nchains))
+    # bytes a sweep touches per study: outcome bits (shared by its chains),
+    # and per chain the coefficients and the FP64 running sums of kept sweeps
+    ws = [st.N * st.V / 8 + c * (st.P * st.V * 4 + (2 * st.P + st.nsubtypes) * st.V * 8)
+          for st, c in zip(studies, nchains)]
     with bsg.Sampler(local) as b:
         for k, (st, nc) in enumerate(zip(studies, nchains)):
             ds = b.add_dataset(st.mask, st.covar, st.data, st.nsubtypes)
@@ -500,8 +510,8 @@ def batched_vs_plain(name: str, local: int) -> dict:
         launches = b.launches_per_sweep()
         # the 16 chains of one study: Gelman-Rubin R-hat of every coefficient
         # map entry across them (the convergence measure reported for it)
-        rhat = (cross_chain_rhat(b, sum(nchains), RHAT_BURNIN, RHAT_SWEEPS)
-                if name == "c4" else None)
+        rh = (cross_chain_rhat(b, sum(nchains), rh_burnin, rh_sweeps)
+              if name == "c4" else None)
     # plain: a lone chain of each study; identical chains of one study cost
     # the same, so a study's nc chains take nc times its lone chain's time
     t_p = 0.0
@@ -517,7 +527,9 @@ def batched_vs_plain(name: str, local: int) -> dict:
             "plain": {"value": upd / (t_p * 1e-3), "ms_per_sweep": t_p,
                       "form": "each chain alone in its own context, bsg_run segments"},
             "batched_over_plain": t_p / t_b, "unit": UNIT, "timing": "device, CUDA events",
-            "clocks": clk.summary(), "rhat": rhat}
+            "working_set_mb": {"batched": sum(ws) / 1e6, "plain_largest": max(ws) / 1e6,
+                               "l2_mb": L2_MB},
+            "clocks": clk.summary(), "rhat": rh}
 
 
 def measure_batched(local: int) -> dict:
@@ -620,75 +632,31 @@ def cross_chain_rhat(s, nchains: int, burnin: int, sweeps: int) -> dict:
 
 
 def run_batched(args, rank, world, local):
-    """Throughput of one context holding every chain of the workload (one
-    batched launch per P group and colour) against the plain form: each
-    single-chain study in its own context, swept one after another with a
-    synchronisation per sweep.  Wall time per sweep, L2 flushed between
-    sweeps."""
+    """One batched workload on its own line (`--workload c0|c3|c4`): every
+    chain / study in one context against the plain single-chain form, both
+    timed as in the default line's `batched` object (batched_vs_plain: graph
+    segments, device time); for c4 the cross-chain R-hat after
+    `--rhat-burnin` + `--rhat-sweeps` sweeps per chain."""
     import torch
-    import bsglmm_gb300 as bsg
     torch.cuda.set_device(local)
-    studies, nchains = batched_workload(args.workload)
-    upd = sum(st.N * st.V * c for st, c in zip(studies, nchains))
-    flushbuf = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
-
-    def timed(samplers, steps):
-        ts = []
-        for _ in range(steps):
-            flush_l2(flushbuf)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            for smp in samplers:
-                smp.run(1, sync=len(samplers) > 1)
-            for smp in samplers:
-                smp.sync()
-            ts.append(time.perf_counter() - t0)
-        return float(np.median(ts))
-
-    batched = bsg.Sampler(local)
-    for k, (st, nc) in enumerate(zip(studies, nchains)):
-        ds = batched.add_dataset(st.mask, st.covar, st.data, st.nsubtypes)
-        for c in range(nc):
-            batched.add_chain(ds, seed=1000 * k + c + 1)
-    for _ in range(args.warmup):
-        batched.run(1)
-    with Clocks(local) as clk:
-        t_b = timed([batched], args.steps)
-    launches = batched.launches_per_sweep()
-    rhat = None
-    if args.workload == "c4":
-        rhat = cross_chain_rhat(batched, sum(nchains), RHAT_BURNIN, RHAT_SWEEPS)
-    batched.close()
-    plain = None
-    if args.workload in ("c0", "c3"):
-        sams = []
-        for k, (st, nc) in enumerate(zip(studies, nchains)):
-            for c in range(nc):
-                smp = bsg.Sampler(local)
-                d = smp.add_dataset(st.mask, st.covar, st.data, st.nsubtypes)
-                smp.add_chain(d, seed=1000 * k + c + 1)
-                sams.append(smp)
-        for smp in sams:
-            smp.run(args.warmup)
-        t_p = timed(sams, max(3, args.steps // 10))
-        for smp in sams:
-            smp.close()
-        plain = {"value": upd / t_p, "ms_per_sweep": t_p * 1e3,
-                 "contexts": len(sams), "launches_per_sweep": 2 * len(sams)}
+    r = batched_vs_plain(args.workload, local, rhat=(args.rhat_burnin, args.rhat_sweeps))
+    b = r["batched"]
     line = {
-        "metric": METRIC, "value": upd / t_b, "unit": UNIT, "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_b * 1e3,
+        "metric": METRIC, "value": b["value"], "unit": UNIT, "n_gpus": 1,
+        "steps": None, "warmup": None, "ms_per_step": b["ms_per_sweep"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (f64 Omega/accumulators)", "data": "synthetic",
-        "config": {"workload": BATCHED[args.workload], "studies": len(studies),
-                   "chains": sum(nchains), "updates_per_sweep": upd,
-                   "voxels": sum(st.V for st in studies),
-                   "l2": "flushed between timed sweeps", "timing": "wall, median"},
-        "sweeps_per_s": 1.0 / t_b, "gpu_launches_per_sweep": launches,
-        "plain": plain,
-        "batched_over_plain": (upd / t_b) / plain["value"] if plain else None,
-        "rhat": rhat,
-        "clocks": clk.summary(),
+        "config": {"workload": r["workload"], "studies": r["studies"],
+                   "chains": r["chains"], "updates_per_sweep": r["updates_per_sweep"],
+                   "segment_sweeps": r["segment_sweeps"],
+                   "l2": "no flush inside a segment; working set %.0f MB batched, %.0f MB for "
+                         "the largest plain study, against a %d MB L2"
+                         % (r["working_set_mb"]["batched"], r["working_set_mb"]["plain_largest"],
+                            L2_MB),
+                   "timing": r["timing"]},
+        "sweeps_per_s": 1e3 / b["ms_per_sweep"], "gpu_launches_per_sweep": b["launches_per_sweep"],
+        "plain": r["plain"], "batched_over_plain": r["batched_over_plain"],
+        "rhat": r["rhat"], "clocks": r["clocks"],
     }
     if rank == 0:
         print(json.dumps(line))
@@ -842,6 +810,10 @@ def main():
     ap.add_argument("--no-tensor-xz", action="store_true")
     ap.add_argument("--tensor-xz", action="store_true",
                     help="model-variant workloads: X'Z on the tensor cores")
+    ap.add_argument("--rhat-burnin", type=int, default=None,
+                    help="--workload c4: burn-in sweeps per chain before the R-hat")
+    ap.add_argument("--rhat-sweeps", type=int, default=None,
+                    help="--workload c4: sweeps per chain behind the R-hat")
     ap.add_argument("--workload", default="brain",
                     choices=["brain", "dic"] + sorted(VARIANTS) + sorted(BATCHED))
     args = ap.parse_args()

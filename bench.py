@@ -55,7 +55,7 @@ CPU_REFERENCE_S = 90.0  # seconds of CPU work in a whole reference-arm run
 # changed since.
 PROFILE = ROOT / "profiles" / "fused_colour_kernel_brain_c1.md"
 KERNEL_SOURCES = ["bsg_fused.cuh", "bsg_device.cuh", "bsg_math.cuh", "bsg_wishart.cuh",
-                  "bsg_internal.h", "bsg_fused_l1.cu", "bsg_mma.cuh"]
+                  "bsg_internal.h", "bsg_fused_l1.cu", "bsg_mma.cuh", "bsg_fused_wide.cu"]
 
 
 def kernel_sources_hash() -> str:
@@ -338,6 +338,7 @@ def run_ours(args, rank, world, local):
     if args.lpv or args.threads:
         s.set_tuning(args.lpv, args.threads)
     lpv, thr = s.tuning()
+    step = s.step_subjects()
     flushbuf = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
 
     # warm-up (also instantiates the one-sweep graph)
@@ -431,6 +432,7 @@ def run_ours(args, rank, world, local):
                    "chains_per_gpu": 1,
                    "l2": "flushed between timed sweeps (value and e2e)",
                    "lanes_per_voxel": lpv, "block_threads": thr,
+                   "subjects_per_step": step,
                    "parallelism": f"replicas x{world}"},
         "sweeps_per_s": 1e3 / ms_per_step,
         "wall_s": wall,

@@ -35,6 +35,8 @@ SIGNATURES = {
     "bsg_set_tuning": (_i32, [_P, _i32, _i32]),
     "bsg_get_tuning": (_i32, [_P, C.POINTER(_i32), C.POINTER(_i32)]),
     "bsg_set_tensor_xz": (_i32, [_P, _i32]),
+    "bsg_set_step_subjects": (_i32, [_P, _i32]),
+    "bsg_get_step_subjects": (_i32, [_P, C.POINTER(_i32)]),
     "bsg_run": (_i32, [_P, _i64]),
     "bsg_sync": (_i32, [_P]),
     "bsg_run_timed": (_i32, [_P, _i64, C.POINTER(C.c_double)]),

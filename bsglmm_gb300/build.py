@@ -31,6 +31,7 @@ SOURCES = [
     "bsg_fused_wm.cu",
     "bsg_fp64.cu",
     "bsg_fused_tc.cu",
+    "bsg_fused_wide.cu",
     "bsg_kernels.cu",
     "bsg_peak.cu",
     "bsg_noalloc.cu",

@@ -17,8 +17,9 @@
 // Work mapping: LPV lanes per voxel; each lane takes whole 32-subject
 // outcome words (w = k, k+LPV, ...) of a subject chunk staged in shared
 // memory, so one Philox call serves four consecutive subjects of one lane
-// (the probit kernel takes two calls, eight subjects, per step, and does
-// its FP32 arithmetic on pairs of subjects with the f32x2 instructions).
+// (the probit kernel takes two or four calls, 8 or 16 subjects, per step,
+// and does its FP32 arithmetic on pairs of subjects with the f32x2
+// instructions).
 #pragma once
 
 #include <type_traits>
@@ -28,18 +29,21 @@
 
 namespace bsg {
 
-// Resident 256-thread blocks per SM asked of ptxas: three (80 registers) up
-// to P = 5, two (128 registers) above, measured fastest on the brain-sized
-// study (P = 5) and the 1.5M-voxel study (P = 6: 2.00 against 2.02 ms per
-// sweep with three blocks, which spill); BSG_FUSED_MIN_BLOCKS overrides it
-// for tuning builds.
-template <int P, bool MIX = false>
+// Resident 256-thread blocks per SM asked of ptxas.  The probit kernel
+// comes in two forms of its whole-word step (below): WIDE draws 16 subjects
+// from four Philox calls at two blocks of 128 registers; the narrow form
+// draws 8 from two calls at three blocks of 80 registers up to P = 5 (two
+// above).  On the brain-sized study (N = 1000, P = 5) WIDE is 6.5 % faster
+// per sweep; on 64 chains of a 50-subject study in one launch the narrow
+// form's extra resident warps win by 27 %.  BSG_FUSED_MIN_BLOCKS overrides
+// it for tuning builds.
+template <int P, bool MIX = false, bool WIDE = false>
 constexpr int fused_min_blocks() {
 #ifdef BSG_FUSED_MIN_BLOCKS
   return BSG_FUSED_MIN_BLOCKS;
 #else
   // the t/logit kernel also keeps the voxel's X' Phi X in registers
-  return MIX ? (P <= 5 ? 2 : 1) : (P <= 5 ? 3 : 2);
+  return MIX ? (P <= 5 ? 2 : 1) : ((WIDE || P > 5) ? 2 : 3);
 #endif
 }
 
@@ -52,14 +56,18 @@ constexpr int fused_min_blocks() {
 // term of its conditional mean through the block partials.
 // TC: the probit kernel's X'(Z - b_WM WM) on the tensor cores as a BF16x3
 // split product (bsg_mma.cuh), one lane per voxel; the rest is unchanged.
-template <int P, int LPV, bool SUPP, bool MIX = false, bool WMU = false, bool TC = false>
-__global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
+// WIDE: the 16-subject whole-word step (identical results).
+template <int P, int LPV, bool SUPP, bool MIX = false, bool WMU = false, bool TC = false,
+          bool WIDE = false>
+__global__ void __launch_bounds__(256, fused_min_blocks<P, MIX, WIDE>())
     fused_colour_kernel(const DatasetDev *__restrict__ dsv,
                         ChainDev *__restrict__ chv,
                         const BlockMap *__restrict__ map, int colour,
                         Supplied sup) {
   static_assert(!TC || (!SUPP && !MIX && !WMU && LPV == 1),
                 "the tensor-core X'Z serves the probit production kernel");
+  static_assert(!WIDE || (!SUPP && !MIX && !TC && LPV == 1),
+                "the 16-subject step serves the probit production kernels");
   constexpr int NT = P * (P + 1) / 2;
   constexpr int PP = P <= 4 ? 4 : 8;  // design row padded to float4s
   // The probit kernel stages the design as subject pairs: pair row m holds
@@ -249,8 +257,13 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
       // f32x2 pairs of subjects (ii0 + 2h, ii0 + 2h + 1); one tail vote for
       // all 4G.  Per subject the same arithmetic as `subject`; the even and
       // odd subjects' X'Z sums are kept apart until the end of the voxel.
-      // G = 2 gives the scheduler four independent pair chains (measured
-      // 1.6 % faster per sweep than G = 1, with identical results).
+      // The whole-word step takes G = kGroups: with WIDE four Philox calls,
+      // 16 subjects, eight independent pair chains for the scheduler (0.527
+      // ms per sweep of the brain-sized study, N = 1000, P = 5, against 0.563
+      // for G = 2 at three resident blocks; the same at P = 8), else two
+      // (G = 2 gives four chains and was measured 1.6 % faster per sweep
+      // than G = 1).  The results do not depend on G.
+      constexpr int kGroups = WIDE ? 4 : 2;
       auto groupp = [&](auto gsz, int ii0, uint32_t ywg, const uint4 *rs, uint32_t i) {
         constexpr int G = decltype(gsz)::value;
         constexpr int H = 2 * G;
@@ -464,13 +477,14 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
           }
           if constexpr (PAIRX) {
 #pragma unroll 1
-            for (int b = 0; b < 32; b += 8) {
+            for (int b = 0; b < 32; b += 4 * kGroups) {
               const uint32_t i = i00 + (uint32_t)b;
-              const uint4 rs[2] = {
-                  philox(make_uint4(i >> 2, (uint32_t)v, sweep, cid | kTagZ), key),
-                  philox(make_uint4((i >> 2) + 1, (uint32_t)v, sweep, cid | kTagZ), key)};
-              groupp(std::integral_constant<int, 2>{}, (wl << 5) + b, yw, rs, i);
-              yw >>= 8;
+              uint4 rs[kGroups];
+#pragma unroll
+              for (int q = 0; q < kGroups; ++q)
+                rs[q] = philox(make_uint4((i >> 2) + q, (uint32_t)v, sweep, cid | kTagZ), key);
+              groupp(std::integral_constant<int, kGroups>{}, (wl << 5) + b, yw, rs, i);
+              yw >>= 4 * kGroups;
               if constexpr (TC) {
                 if (b & 8) {  // a 16-subject slice is complete
                   __syncwarp();
@@ -871,7 +885,8 @@ __global__ void __launch_bounds__(256, fused_min_blocks<P, MIX>())
 // programmatic-stream-serialization attribute, so it may start once every
 // block of the previous kernel in the stream has passed its dependency
 // point.
-template <int P, int LPV, bool SUPP, bool MIX = false, bool WMU = false, bool TC = false>
+template <int P, int LPV, bool SUPP, bool MIX = false, bool WMU = false, bool TC = false,
+          bool WIDE = false>
 cudaError_t launch_one(int nblocks, int threads, cudaStream_t st, bool pdl,
                        const DatasetDev *ds, ChainDev *ch, const BlockMap *map,
                        int colour, const Supplied &sup) {
@@ -888,8 +903,8 @@ cudaError_t launch_one(int nblocks, int threads, cudaStream_t st, bool pdl,
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = pdl ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, fused_colour_kernel<P, LPV, SUPP, MIX, WMU, TC>, ds, ch,
-                            map, colour, sup);
+  return cudaLaunchKernelEx(&cfg, fused_colour_kernel<P, LPV, SUPP, MIX, WMU, TC, WIDE>, ds,
+                            ch, map, colour, sup);
 }
 
 // The dynamic shared memory opt-in of one tensor-core instantiation.

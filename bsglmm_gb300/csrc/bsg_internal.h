@@ -161,6 +161,11 @@ cudaError_t launch_fused_tc(int P, int threads, const DatasetDev *ds, ChainDev *
                             bool pdl);
 // Its dynamic shared memory opt-in, before the first launch on a device.
 cudaError_t prepare_fused_tc();
+// The probit colour kernel (wmu: with the beta_WM update) on the 16-subject
+// whole-word step, one lane per voxel, Philox (bsg_fused_wide.cu).
+cudaError_t launch_fused_wide(int P, int threads, bool wmu, const DatasetDev *ds,
+                              ChainDev *ch, const BlockMap *map, int nblocks, int colour,
+                              cudaStream_t st, bool pdl);
 // The colour kernel of FP64 chains (bsg_fp64.cu): one thread per voxel,
 // kF64Threads voxels per block, Philox variates, probit link.
 cudaError_t launch_fp64(int P, const DatasetDev *ds, ChainDev *ch, const BlockMap *map,

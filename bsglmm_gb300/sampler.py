@@ -107,6 +107,18 @@ class Sampler:
         self._check(self._L.bsg_set_tensor_xz(self._h, int(bool(enable))),
                     "bsg_set_tensor_xz")
 
+    def set_step_subjects(self, subjects: int = 0):
+        """Subjects per whole-word step of the probit colour kernel: 8, 16,
+        or 0 to choose per P group (identical results either way)."""
+        self._check(self._L.bsg_set_step_subjects(self._h, int(subjects)),
+                    "bsg_set_step_subjects")
+
+    def step_subjects(self) -> int:
+        n = C.c_int32()
+        self._check(self._L.bsg_get_step_subjects(self._h, C.byref(n)),
+                    "bsg_get_step_subjects")
+        return n.value
+
     def tuning(self):
         a, b = C.c_int32(), C.c_int32()
         self._check(self._L.bsg_get_tuning(self._h, C.byref(a), C.byref(b)),

@@ -103,6 +103,18 @@ bsg_status bsg_get_tuning(const bsg_ctx *ctx, int32_t *lanes_per_voxel,
  * 2^-16 relative per product).  No counterpart in the reference. */
 bsg_status bsg_set_tensor_xz(bsg_ctx *ctx, int32_t enable);
 
+/* Subjects per whole-word step of the probit colour kernel (with or without
+ * the beta_WM update; one lane per voxel, SIMT X'Z): 16 draws four Philox
+ * calls per step at two resident blocks of 128 registers, 8 draws two at
+ * three blocks of 80 (P <= 5).  0 (the default) chooses per P group: 16
+ * when P > 5, when the group's chains average N >= 384 subjects per voxel,
+ * or when its grid is at most two blocks per SM; else 8.  The variates and
+ * the arithmetic are the same, so the results are identical bit for bit.
+ * bsg_get_step_subjects gives the largest step the context's plan uses
+ * (0 when no chain is probit FP32).  No counterpart in the reference. */
+bsg_status bsg_set_step_subjects(bsg_ctx *ctx, int32_t subjects);
+bsg_status bsg_get_step_subjects(bsg_ctx *ctx, int32_t *subjects);
+
 /* ------------------------------------------------------------ sampling -- */
 /* Advances every chain by nsweeps sweeps (one sweep = latent Z + beta for
  * both colours, the Omega Wishart draw, and on kept sweeps the posterior
@@ -230,9 +242,10 @@ bsg_status bsg_checkpoint(bsg_ctx *ctx, int32_t chain, void *buf, int64_t size);
 bsg_status bsg_restore(bsg_ctx *ctx, int32_t chain, const void *buf,
                        int64_t size);
 /* Times each supported tile shape (lanes per voxel x threads per block,
- * and at one lane per voxel both X'Z paths of bsg_set_tensor_xz) on the
- * context's chains for `sweeps` sweeps, keeps the fastest (the X'Z path
- * stays set on the context) and puts every chain back to its state before
+ * and at one lane per voxel both X'Z paths of bsg_set_tensor_xz and, on
+ * the SIMT path, both steps of bsg_set_step_subjects) on the context's
+ * chains for `sweeps` sweeps, keeps the fastest (the X'Z path and the step
+ * stay set on the context) and puts every chain back to its state before
  * the call. */
 bsg_status bsg_autotune(bsg_ctx *ctx, int32_t sweeps, int32_t *lanes_per_voxel,
                         int32_t *block_threads);

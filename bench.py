@@ -10,9 +10,10 @@ P = 5 covariates, single chain, FP32 sweep with FP64 Omega/accumulators.
 Prints one JSON line.  `value` is subject*voxel updates per second with the
 study resident in HBM (device time of the K timed sweeps, L2 flushed between
 sweeps); `e2e` is the same metric through the C ABI with host buffers: each
-step uploads the chain's Omega from host memory (as the reference's
-updateSpatCoefGPU does, covarGPU.cu:540) and reads the new Omega and the
-column means back (covarGPU.cu:582,1106-1108).  With N > 1 (torchrun) every
+step is one bsg_step_host call that uploads the chain's Omega from host
+memory (as the reference's updateSpatCoefGPU does, covarGPU.cu:540), runs the
+sweep and reads the new Omega and the column means back
+(covarGPU.cu:582,1106-1108).  With N > 1 (torchrun) every
 rank runs an independent chain on its own GPU (replicas, weak scaling).
 `--impl reference` times the reference's CPU sweep (the oracle's timing port
 of covar.cpp's updateZ / updateSpatCoef / updateSpatCoefPrec) on all host
@@ -369,24 +370,36 @@ def run_ours(args, rank, world, local):
 
     # e2e through the C ABI with host buffers (Omega in, Omega + column means
     # out), wall time of each step from the host; L2 is flushed before each
-    # step, outside its timed interval, as for `value`
+    # step, outside its timed interval, as for `value`.  The step is one
+    # bsg_step_host call; the same round trip as four calls (set Omega, run,
+    # get Omega, get column means: what the covarGPU.cu shim does) is timed
+    # beside it.
     om = s.omega(ch)
     h2d = om.nbytes
     d2h = om.nbytes + 4 * P
+    out = (np.empty_like(om), np.empty(P, np.float32))
     barrier()
-    e2e_local = 0.0
-    for _ in range(args.steps):
-        flush_l2(flushbuf)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        s.set_omega(ch, om)
-        s.run(1, sync=False)
-        om = s.omega(ch)      # waits for the sweep
-        _ = s.colmeans(ch)
-        e2e_local += time.perf_counter() - t0
-    s.sync()
-    e2e_s = reduce_max(e2e_local, world)
-    e2e = world * N * V * args.steps / e2e_s
+
+    def e2e_steps(one_call):
+        nonlocal om
+        t = 0.0
+        for _ in range(args.steps):
+            flush_l2(flushbuf)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if one_call:
+                om = s.step_host(ch, om, 1, out=out)[0]
+            else:
+                s.set_omega(ch, om)
+                s.run(1, sync=False)
+                om = s.omega(ch)      # waits for the sweep
+                _ = s.colmeans(ch)
+            t += time.perf_counter() - t0
+        s.sync()
+        return world * N * V * args.steps / reduce_max(t, world)
+
+    e2e = e2e_steps(True)
+    e2e_calls = e2e_steps(False)
 
     # live per-kernel timing of the same sweep (CUDA events on the sampler's
     # stream, plain launches)
@@ -437,7 +450,10 @@ def run_ours(args, rank, world, local):
         "sweeps_per_s": 1e3 / ms_per_step,
         "wall_s": wall,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+                "d2h_bytes_per_step": d2h,
+                "form": "one bsg_step_host call per sweep (Omega in; Omega and column "
+                        "means out)",
+                "four_calls_value": e2e_calls},
         "gpu_launches": launches,
         "roofline": {
             "bound": "fp32", "kernel": "fused_colour_kernel",

@@ -40,6 +40,7 @@ SIGNATURES = {
     "bsg_run": (_i32, [_P, _i64]),
     "bsg_sync": (_i32, [_P]),
     "bsg_run_timed": (_i32, [_P, _i64, C.POINTER(C.c_double)]),
+    "bsg_step_host": (_i32, [_P, _i32, _P, _i64, _P, _P]),
     "bsg_profile": (_i32, [_P, _i64, _P, _P]),
     "bsg_launches_per_sweep": (_i64, [_P]),
     "bsg_stream": (_P, [_P]),

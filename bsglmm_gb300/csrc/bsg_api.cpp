@@ -111,6 +111,8 @@ struct bsg_ctx {
                     // previous kernel's tail (programmatic dependent launch)
 #endif
   std::map<int64_t, cudaGraphExec_t> graphs;
+  void *pin = nullptr;  // pinned staging of bsg_step_host
+  size_t pin_bytes = 0;
   std::string err;
 };
 
@@ -663,6 +665,7 @@ bsg_status bsg_destroy(bsg_ctx *ctx) {
   for (auto e : ctx->join) cudaEventDestroy(e);
   if (ctx->fork) cudaEventDestroy(ctx->fork);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->pin) cudaFreeHost(ctx->pin);
   delete ctx;
   return BSG_OK;
 }
@@ -996,6 +999,54 @@ bsg_status bsg_sync(bsg_ctx *ctx) {
     }
     return status_from_bits(bits);
   }
+  return BSG_OK;
+}
+
+bsg_status bsg_step_host(bsg_ctx *ctx, int32_t chain, const double *omega_in,
+                         int64_t nsweeps, double *omega_out, float *colmeans_out) {
+  if (!valid_chain(ctx, chain) || nsweeps < 0) return BSG_ERR_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  bsg_status s = build_plan(ctx);
+  if (s) return s;
+  const Chain &c = ctx->ch[chain];
+  const int P = ctx->ds[c.dataset].P;
+  // staging: Omega in (FP64, FP32), Omega out, column means, status word
+  const size_t nd = sizeof(double) * P * P, nf = sizeof(float) * P * P;
+  const size_t need = 2 * nd + nf + sizeof(float) * P + sizeof(int);
+  if (ctx->pin_bytes < need) {
+    // nothing in flight reads the old buffer: every call ends synchronised
+    if (ctx->pin) CK(cudaFreeHost(ctx->pin));
+    ctx->pin = nullptr;
+    ctx->pin_bytes = 0;
+    CK(cudaHostAlloc(&ctx->pin, need, cudaHostAllocDefault));
+    ctx->pin_bytes = need;
+  }
+  char *base = (char *)ctx->pin;
+  double *in_d = (double *)base, *out_d = (double *)(base + nd);
+  float *in_f = (float *)(base + 2 * nd), *cm = (float *)(base + 2 * nd + nf);
+  int *bits = (int *)(base + 2 * nd + nf + sizeof(float) * P);
+  if (omega_in) {
+    for (int i = 0; i < P * P; ++i) {
+      in_d[i] = omega_in[i];
+      in_f[i] = (float)omega_in[i];
+    }
+    CK(cudaMemcpyAsync(c.dev.omega_d, in_d, nd, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(c.dev.omega_f, in_f, nf, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  if (nsweeps > 0 && (s = bsg_run(ctx, nsweeps))) return s;
+  if (omega_out)
+    CK(cudaMemcpyAsync(out_d, c.dev.omega_d, nd, cudaMemcpyDeviceToHost, ctx->stream));
+  if (colmeans_out)
+    CK(cudaMemcpyAsync(cm, c.dev.colmean, sizeof(float) * P, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+  *bits = 0;
+  if (ctx->any_status)
+    CK(cudaMemcpyAsync(bits, ctx->any_status, sizeof(int), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (*bits) return bsg_sync(ctx);  // names the failing chains
+  if (omega_out) std::memcpy(omega_out, out_d, nd);
+  if (colmeans_out) std::memcpy(colmeans_out, cm, sizeof(float) * P);
   return BSG_OK;
 }
 

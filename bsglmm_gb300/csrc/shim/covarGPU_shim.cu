@@ -58,6 +58,8 @@ struct ShimState {
   bool failed = false;
   bool wm_update = false;  // updateBetaGPU has been called
   bool wm_on = false;      // the chain draws beta_WM
+  std::vector<double> omega;  // Omega after the last sweep (bsg_step_host)
+  bool omega_valid = false;
 };
 ShimState g;
 
@@ -137,23 +139,28 @@ void updateSpatCoefGPU(float *covar, float *, float *, float *SpatCoefPrec,
   const int P = NCOVAR;
   std::vector<double> om((size_t)P * P);
   for (int i = 0; i < P * P; ++i) om[i] = (double)SpatCoefPrec[i];
-  report("bsg_set_omega", bsg_set_omega(g.ctx, g.ch, om.data()));
   // with the beta_WM update on, the device value (drawn at the end of each
   // sweep) is the chain's; the host copy is one draw behind
   if (!g.wm_on) report("bsg_set_beta_wm", bsg_set_beta_wm(g.ctx, g.ch, beta));
-  report("bsg_run", bsg_run(g.ctx, 1));
-  report("bsg_sync", bsg_sync(g.ctx));
+  // Omega in, the sweep, the new Omega (kept for updateSpatCoefPrecGPU) and
+  // the column means out: one call, one wait
+  g.omega.resize((size_t)P * P);
   std::vector<float> cm(P);
-  report("bsg_get_colmeans", bsg_get_colmeans(g.ctx, g.ch, cm.data()));
+  const bsg_status s = bsg_step_host(g.ctx, g.ch, om.data(), 1, g.omega.data(), cm.data());
+  report("bsg_step_host", s);
+  g.omega_valid = s == BSG_OK;
   for (int p = 0; p < P; ++p) alphaMean[p] = cm[p] / logit_factor;
 }
 
 void updateSpatCoefPrecGPU(float *SpatCoefPrec, unsigned long *seed) {
   if (!g.ctx) return;
   const int P = NCOVAR;
-  std::vector<double> om((size_t)P * P);
-  report("bsg_get_omega", bsg_get_omega(g.ctx, g.ch, om.data()));
-  for (int i = 0; i < P * P; ++i) SpatCoefPrec[i] = (float)om[i];
+  if (!g.omega_valid) {
+    g.omega.resize((size_t)P * P);
+    report("bsg_get_omega", bsg_get_omega(g.ctx, g.ch, g.omega.data()));
+  }
+  for (int i = 0; i < P * P; ++i) SpatCoefPrec[i] = (float)g.omega[i];
+  g.omega_valid = false;
   kiss(seed);  // the reference's Wishart draw consumes the host stream
 }
 

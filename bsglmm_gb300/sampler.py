@@ -134,6 +134,21 @@ class Sampler:
         if sync:
             self.sync()
 
+    def step_host(self, chain: int, omega=None, nsweeps: int = 1, out=None):
+        """One call: Omega in (None keeps the chain's), nsweeps sweeps of
+        every chain, the chain's Omega and column means out, one wait
+        (bsg_step_host).  `out` = (omega [P][P] float64, colmeans [P]
+        float32) arrays to fill, else new ones."""
+        P = self._dims(chain)["P"]
+        a = None if omega is None else np.ascontiguousarray(omega, dtype=np.float64)
+        if a is not None and a.size != P * P:
+            raise ValueError(f"omega must have {P * P} entries")
+        om, cm = out if out is not None else (np.empty((P, P), np.float64),
+                                              np.empty(P, np.float32))
+        self._check(self._L.bsg_step_host(self._h, chain, _ptr(a), int(nsweeps),
+                                          _ptr(om), _ptr(cm)), "bsg_step_host")
+        return om, cm
+
     def sync(self):
         self._check(self._L.bsg_sync(self._h), "bsg_sync")
 

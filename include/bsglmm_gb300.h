@@ -122,6 +122,17 @@ bsg_status bsg_get_step_subjects(bsg_ctx *ctx, int32_t *subjects);
 bsg_status bsg_run(bsg_ctx *ctx, int64_t nsweeps);
 /* Waits for the context's stream; returns the first sampler error seen. */
 bsg_status bsg_sync(bsg_ctx *ctx);
+/* One host-driven step of one chain, the round trip the reference makes
+ * per sweep (updateSpatCoefGPU uploads Omega and reads the column means,
+ * updateSpatCoefPrecGPU reads the new Omega: covarGPU.cu:540,582,1106-1108)
+ * in a single call: Omega from omega_in (P x P, NULL keeps the chain's),
+ * nsweeps sweeps of every chain as bsg_run, then the chain's Omega and
+ * column means into omega_out / colmeans_out (either may be NULL).  The
+ * copies go through a pinned staging buffer of the context and the call
+ * waits once, at the end, for the stream; it returns the first sampler
+ * error seen, as bsg_sync does. */
+bsg_status bsg_step_host(bsg_ctx *ctx, int32_t chain, const double *omega_in,
+                         int64_t nsweeps, double *omega_out, float *colmeans_out);
 /* Runs nsweeps and reports elapsed device time (CUDA events on the
  * context's stream around the whole batch). */
 bsg_status bsg_run_timed(bsg_ctx *ctx, int64_t nsweeps, double *ms);

@@ -111,23 +111,76 @@ def dist_env():
     return rank, world, local
 
 
+class _Nvml:
+    """Read-only NVML queries through the driver's libnvidia-ml (ctypes): the
+    SM clock, its maximum and the active clock-event reasons of one GPU."""
+
+    SM = 1  # NVML_CLOCK_SM
+    BITS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+            0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, target: str):
+        import ctypes as C
+        self.C = C
+        self.lib = C.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit_v2")
+        self.h = C.c_void_p()
+        if target.isdigit():
+            st = self.lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(int(target)), C.byref(self.h))
+        else:
+            st = self.lib.nvmlDeviceGetHandleByUUID(target.encode(), C.byref(self.h))
+        if st != 0:
+            raise OSError("no NVML handle for GPU " + target)
+        mx = C.c_uint()
+        self.max_mhz = (float(mx.value) if self.lib.nvmlDeviceGetMaxClockInfo(
+            self.h, self.SM, C.byref(mx)) == 0 else None)
+        self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) \
+            or self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def sample(self):
+        C = self.C
+        clk, r = C.c_uint(), C.c_ulonglong()
+        if self.lib.nvmlDeviceGetClockInfo(self.h, self.SM, C.byref(clk)) != 0:
+            return None
+        bits = r.value if self.reasons_fn(self.h, C.byref(r)) == 0 else 0
+        return float(clk.value), {n for b, n in self.BITS.items() if bits & b}
+
+
 class Clocks:
-    """Samples SM clocks and throttle reasons with nvidia-smi while the
-    timed region runs."""
+    """Samples SM clocks and clock-event (throttle) reasons while the timed
+    region runs: NVML every millisecond where the driver's library loads
+    (a timed region of a few milliseconds still gets several readings), else
+    nvidia-smi every 50 ms.  Only reads the settings."""
 
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index: int):
-        self.index = index
+        # the GPU as NVML and nvidia-smi number it: CUDA's device `index`
+        # is an entry of CUDA_VISIBLE_DEVICES when that is set
+        vis = [x.strip() for x in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")
+               if x.strip()]
+        self.index = vis[index] if index < len(vis) else str(index)
         self.proc = None
+        self.nvml = None
         self.lines = []
+        self.samples = []
+        self._stop = threading.Event()
 
     def __enter__(self):
         try:
+            self.nvml = _Nvml(self.index)
+        except (OSError, AttributeError):
+            self.nvml = None
+        if self.nvml:
+            self._t = threading.Thread(target=self._poll, daemon=True)
+            self._t.start()
+            return self
+        try:
             self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                ["nvidia-smi", "-i", self.index, f"--query-gpu={self.Q}",
                  "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
@@ -136,11 +189,22 @@ class Clocks:
             self.proc = None
         return self
 
+    def _poll(self):
+        while True:
+            x = self.nvml.sample()
+            if x:
+                self.samples.append(x)
+            if self._stop.wait(0.001):
+                return
+
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        self._stop.set()
+        if self.nvml:
+            self._t.join(timeout=5)
         if self.proc:
             self.proc.terminate()
             try:
@@ -149,6 +213,12 @@ class Clocks:
                 self.proc.kill()
 
     def summary(self):
+        if self.nvml:
+            sm = [c for c, _ in self.samples]
+            reasons = set().union(*[r for _, r in self.samples]) if self.samples else set()
+            return {"sm_mhz": statistics.median(sm) if sm else None,
+                    "sm_max_mhz": self.nvml.max_mhz, "samples": len(sm),
+                    "reasons": sorted(reasons), "source": "NVML, 1 ms"}
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
                  "sw_power_cap"]
@@ -165,7 +235,8 @@ class Clocks:
                 if v.lower() == "active":
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None,
-                "sm_max_mhz": mx, "samples": len(sm), "reasons": sorted(reasons)}
+                "sm_max_mhz": mx, "samples": len(sm), "reasons": sorted(reasons),
+                "source": "nvidia-smi, 50 ms"}
 
 
 def issue_roofline(device: int, updates_per_s: float, prof: dict):

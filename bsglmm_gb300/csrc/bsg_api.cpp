@@ -1595,7 +1595,8 @@ bsg_status bsg_autotune(bsg_ctx *ctx, int32_t sweeps, int32_t *best_lpv,
   for (int lpv : lpvs)
     for (int thr : thrs)
       for (int tc = 0; tc < (lpv == 1 ? 2 : 1); ++tc)  // X'Z: SIMT, tensor cores
-        for (int step = 8; step <= (lpv == 1 && !tc ? 16 : 8); step += 8) {
+        for (int step : {0, 16, 8}) {  // subjects per step: per group, 16, 8
+          if (step && (lpv != 1 || tc)) continue;  // those take the 8-subject step
           if (thr / lpv < 8) continue;
           bsg_status s = bsg_set_tuning(ctx, lpv, thr);
           if (!s) s = bsg_set_tensor_xz(ctx, tc);

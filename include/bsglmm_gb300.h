@@ -254,10 +254,10 @@ bsg_status bsg_restore(bsg_ctx *ctx, int32_t chain, const void *buf,
                        int64_t size);
 /* Times each supported tile shape (lanes per voxel x threads per block,
  * and at one lane per voxel both X'Z paths of bsg_set_tensor_xz and, on
- * the SIMT path, both steps of bsg_set_step_subjects) on the context's
- * chains for `sweeps` sweeps, keeps the fastest (the X'Z path and the step
- * stay set on the context) and puts every chain back to its state before
- * the call. */
+ * the SIMT path, the settings 0, 16 and 8 of bsg_set_step_subjects) on the
+ * context's chains for `sweeps` sweeps, keeps the fastest (the X'Z path and
+ * the step setting stay set on the context) and puts every chain back to
+ * its state before the call. */
 bsg_status bsg_autotune(bsg_ctx *ctx, int32_t sweeps, int32_t *lanes_per_voxel,
                         int32_t *block_threads);
 

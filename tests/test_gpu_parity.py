@@ -315,5 +315,6 @@ def test_autotune_restores_state(bsg):
         b0, o0, sw0 = s.beta(ch), s.omega(ch), s.sweep_count(ch)
         lpv, thr = s.autotune(2)
         assert (lpv, thr) == s.tuning()
+        assert s.step_subjects() in (8, 16)
         assert np.array_equal(s.beta(ch), b0) and np.array_equal(s.omega(ch), o0)
         assert s.sweep_count(ch) == sw0

@@ -113,6 +113,7 @@ struct bsg_ctx {
   std::map<int64_t, cudaGraphExec_t> graphs;
   void *pin = nullptr;  // pinned staging of bsg_step_host
   size_t pin_bytes = 0;
+  bool pin_busy = false;  // copies through it may be in flight (a call ended early)
   std::string err;
 };
 
@@ -1013,8 +1014,11 @@ bsg_status bsg_step_host(bsg_ctx *ctx, int32_t chain, const double *omega_in,
   // staging: Omega in (FP64, FP32), Omega out, column means, status word
   const size_t nd = sizeof(double) * P * P, nf = sizeof(float) * P * P;
   const size_t need = 2 * nd + nf + sizeof(float) * P + sizeof(int);
+  if (ctx->pin_busy) {  // a previous call returned before its copies finished
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->pin_busy = false;
+  }
   if (ctx->pin_bytes < need) {
-    // nothing in flight reads the old buffer: every call ends synchronised
     if (ctx->pin) CK(cudaFreeHost(ctx->pin));
     ctx->pin = nullptr;
     ctx->pin_bytes = 0;
@@ -1025,6 +1029,7 @@ bsg_status bsg_step_host(bsg_ctx *ctx, int32_t chain, const double *omega_in,
   double *in_d = (double *)base, *out_d = (double *)(base + nd);
   float *in_f = (float *)(base + 2 * nd), *cm = (float *)(base + 2 * nd + nf);
   int *bits = (int *)(base + 2 * nd + nf + sizeof(float) * P);
+  ctx->pin_busy = true;
   if (omega_in) {
     for (int i = 0; i < P * P; ++i) {
       in_d[i] = omega_in[i];
@@ -1044,6 +1049,7 @@ bsg_status bsg_step_host(bsg_ctx *ctx, int32_t chain, const double *omega_in,
     CK(cudaMemcpyAsync(bits, ctx->any_status, sizeof(int), cudaMemcpyDeviceToHost,
                        ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  ctx->pin_busy = false;
   if (*bits) return bsg_sync(ctx);  // names the failing chains
   if (omega_out) std::memcpy(omega_out, out_d, nd);
   if (colmeans_out) std::memcpy(colmeans_out, cm, sizeof(float) * P);

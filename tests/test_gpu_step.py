@@ -87,3 +87,23 @@ def test_auto_choice_and_refusal():
         s.add_chain(ds, seed=1)
         with pytest.raises(RuntimeError):
             s.set_step_subjects(12)
+
+
+def test_per_group_choice_on_the_benchmark_studies():
+    """16 subjects for one chain of the brain-sized study (N = 1000); 8 for
+    64 chains of the 20^3 study (N = 50), whose grid fills the GPU."""
+    import bsglmm_gb300 as bsg
+    from bsglmm_gb300 import synth
+    brain = synth.config1(seed=1)
+    with bsg.Sampler() as s:
+        s.add_chain(s.add_dataset(brain.mask, brain.covar, brain.data, brain.nsubtypes),
+                    seed=1)
+        assert s.step_subjects() == 16
+    small = synth.config0(0)
+    with bsg.Sampler() as s:
+        ds = s.add_dataset(small.mask, small.covar, small.data, small.nsubtypes)
+        for c in range(64):
+            s.add_chain(ds, seed=1 + c)
+        assert s.step_subjects() == 8
+        s.set_step_subjects(16)
+        assert s.step_subjects() == 16
